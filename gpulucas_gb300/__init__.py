@@ -1,0 +1,292 @@
+"""gpulucas_gb300 -- GB300-native Lucas-Lehmer engine (IBDWT, FP64, sm_103a kernels).
+
+Python mirror of the reference's entry points over the C ABI (include/gpulucas.h):
+
+* ``mersenneTest(p, N)``  -- full test (gpuLucas.cu:1358-1551, README errorTest/mersenneTest)
+* ``errorTest(p, N)``     -- timing/round-off trial (errorTrial, gpuLucas.cu:1192-1282)
+* ``setSliceAndDice(p, N)`` -- carry depth n of llintToIrrBal<n> (gpuLucas.cu:323-343)
+* ``Plan``               -- a per-test plan: iterate, products, carry state, residue
+
+All compute runs in ``libgpulucas_gb300.so``; there is no CPU fallback.  Importing this
+package without the built library raises ImportError (run ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgpulucas_gb300.so")
+
+GL_OK = 0
+GL_ERR_ARG = -1
+GL_ERR_RATIO = -2
+GL_ERR_SIZE = -3
+GL_ERR_CUDA = -4
+GL_ERR_NOMEM = -5
+GL_ERR_ROUNDOFF = -6
+GL_ERR_OVERFLOW = -7
+GL_ERR_NODEVICE = -8
+GL_ERR_IO = -9
+GL_ERR_CHECKPOINT = -10
+GL_ERR_STATE = -11
+
+MODE_FUSED = 0
+MODE_PLAIN = 1
+
+
+class PlanOpts(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("device", ctypes.c_int), ("error_limit", ctypes.c_double),
+                ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
+                ("cols_per_cta", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_int), ("N", ctypes.c_int), ("lo_bits", ctypes.c_int), ("hi_bits", ctypes.c_int),
+                ("carry_depth", ctypes.c_int), ("mode", ctypes.c_int), ("fft_w", ctypes.c_int),
+                ("fft_h", ctypes.c_int), ("cols_per_cta", ctypes.c_int), ("radix_w", ctypes.c_int * 8),
+                ("radix_h", ctypes.c_int * 8), ("threads_col", ctypes.c_int), ("threads_row", ctypes.c_int),
+                ("smem_col", ctypes.c_int), ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t)]
+
+
+class IterReport(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("total_iterations", ctypes.c_int64),
+                ("max_roundoff", ctypes.c_double), ("ms", ctypes.c_double), ("status", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_int), ("N", ctypes.c_int), ("iterations", ctypes.c_int64),
+                ("is_prime", ctypes.c_int), ("is_zero", ctypes.c_int), ("res64", ctypes.c_uint64),
+                ("max_roundoff", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build() "
+                          "(this package has no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    vp = ctypes.c_void_p
+    sig = {
+        "gl_default_opts": (ctypes.c_int, [ctypes.POINTER(PlanOpts)]),
+        "gl_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
+        "gl_plan_destroy": (ctypes.c_int, [P]),
+        "gl_plan_get_info": (ctypes.c_int, [P, ctypes.POINTER(PlanInfo)]),
+        "gl_plan_describe": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PlanOpts),
+                                            ctypes.POINTER(PlanInfo)]),
+        "gl_reset": (ctypes.c_int, [P]),
+        "gl_iterate": (ctypes.c_int, [P, ctypes.c_int64, ctypes.POINTER(IterReport)]),
+        "gl_plan_stream": (ctypes.c_int, [P, PP]),
+        "gl_enqueue": (ctypes.c_int, [P, ctypes.c_int64]),
+        "gl_sync_status": (ctypes.c_int, [P, ctypes.POINTER(IterReport)]),
+        "gl_launches_per_iteration": (ctypes.c_int, [P]),
+        "gl_get_products": (ctypes.c_int, [P, vp]),
+        "gl_get_carry_state": (ctypes.c_int, [P, vp, vp]),
+        "gl_set_products": (ctypes.c_int, [P, vp, ctypes.c_int64]),
+        "gl_set_carry_state": (ctypes.c_int, [P, vp, vp, ctypes.c_int64]),
+        "gl_get_residue": (ctypes.c_int, [P, vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
+        "errorTest": (ctypes.c_float, [ctypes.c_int, ctypes.c_int]),
+        "mersenneTest": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+        "setSliceAndDice": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+        "gl_error_test": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.c_int,
+                                         ctypes.POINTER(IterReport)]),
+        "gl_mersenne_test": (ctypes.c_int, [P, ctypes.c_int64, ctypes.POINTER(Result)]),
+        "gl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
+        "gl_version": (ctypes.c_int, []),
+        "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+lib = _load()
+
+# exported C symbols that include/gpulucas.h declares (checked by the tests)
+ABI_SYMBOLS = tuple(sorted([
+    "gl_default_opts", "gl_plan_create", "gl_plan_destroy", "gl_plan_get_info", "gl_plan_describe",
+    "gl_reset", "gl_iterate",
+    "gl_plan_stream", "gl_enqueue", "gl_sync_status", "gl_launches_per_iteration", "gl_get_products",
+    "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
+    "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
+    "gl_probe_fp64_peak",
+]))
+
+
+class GLError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = lib.gl_error_string(status).decode()
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+def _check(status: int, what: str) -> int:
+    if status < 0:
+        raise GLError(status, what)
+    return status
+
+
+def default_opts(**kw) -> PlanOpts:
+    o = PlanOpts()
+    lib.gl_default_opts(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown plan option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Plan:
+    """One Lucas-Lehmer test of 2^p - 1 at FFT length N on one GPU."""
+
+    def __init__(self, p: int, N: int, mode: int = MODE_FUSED, **opts):
+        self.p, self.N = int(p), int(N)
+        o = default_opts(mode=mode, **opts)
+        h = ctypes.c_void_p()
+        _check(lib.gl_plan_create(self.p, self.N, ctypes.byref(o), ctypes.byref(h)), f"plan p={p} N={N}")
+        self._h = h
+        info = PlanInfo()
+        _check(lib.gl_plan_get_info(self._h, ctypes.byref(info)), "plan info")
+        self.info = info
+
+    # lifetime -----------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.gl_plan_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # state -------------------------------------------------------------------
+    def reset(self):
+        _check(lib.gl_reset(self._h), "reset")
+
+    def iterate(self, iters: int, check: bool = True) -> IterReport:
+        rep = IterReport()
+        st = lib.gl_iterate(self._h, int(iters), ctypes.byref(rep))
+        if check:
+            _check(st, "iterate")
+        return rep
+
+    def enqueue(self, iters: int):
+        _check(lib.gl_enqueue(self._h, int(iters)), "enqueue")
+
+    def sync_status(self, check: bool = True) -> IterReport:
+        rep = IterReport()
+        st = lib.gl_sync_status(self._h, ctypes.byref(rep))
+        if check:
+            _check(st, "status")
+        return rep
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _check(lib.gl_plan_stream(self._h, ctypes.byref(s)), "stream")
+        return s.value or 0
+
+    @property
+    def launches_per_iteration(self) -> int:
+        return _check(lib.gl_launches_per_iteration(self._h), "launches")
+
+    def products(self) -> np.ndarray:
+        out = np.empty(self.N, np.int64)
+        _check(lib.gl_get_products(self._h, _ptr(out)), "products")
+        return out
+
+    def set_products(self, ll: np.ndarray, iterations: int = 0):
+        ll = np.ascontiguousarray(ll, np.int64)
+        assert ll.shape == (self.N,)
+        _check(lib.gl_set_products(self._h, _ptr(ll), int(iterations)), "set_products")
+
+    def carry_state(self):
+        d = np.empty(self.N, np.int32)
+        h = np.empty(self.N, np.int8)
+        _check(lib.gl_get_carry_state(self._h, _ptr(d), _ptr(h)), "carry_state")
+        return d, h
+
+    def set_carry_state(self, digit: np.ndarray, hi: np.ndarray, iterations: int):
+        d = np.ascontiguousarray(digit, np.int32)
+        h = np.ascontiguousarray(hi, np.int8)
+        _check(lib.gl_set_carry_state(self._h, _ptr(d), _ptr(h), int(iterations)), "set_carry_state")
+
+    def residue(self):
+        """(rebalanced digits, res64, is_zero) of the current state."""
+        d = np.empty(self.N, np.int32)
+        r = ctypes.c_uint64()
+        z = ctypes.c_int()
+        _check(lib.gl_get_residue(self._h, _ptr(d), ctypes.byref(r), ctypes.byref(z)), "residue")
+        return d, int(r.value), bool(z.value)
+
+    def res64(self) -> int:
+        return self.residue()[1]
+
+    def mersenne_test(self, iters: int = 0) -> Result:
+        res = Result()
+        st = lib.gl_mersenne_test(self._h, int(iters), ctypes.byref(res))
+        _check(st, "mersenne_test")
+        return res
+
+
+# reference-named entry points ---------------------------------------------------
+
+def mersenneTest(testPrime: int, signalSize: int) -> int:
+    """1 if 2^p - 1 is prime, 0 if composite (prints the reference's result line)."""
+    return _check(lib.mersenneTest(int(testPrime), int(signalSize)), "mersenneTest")
+
+
+def errorTest(testPrime: int, signalSize: int) -> float:
+    """Average ms per iteration over clamp(p/10000, 100, 2500) iterations, -1 on error."""
+    return float(lib.errorTest(int(testPrime), int(signalSize)))
+
+
+def setSliceAndDice(testPrime: int, signalSize: int) -> int:
+    """Carry depth n of llintToIrrBal<n> for p/N; raises for ratio >= 22."""
+    return _check(lib.setSliceAndDice(int(testPrime), int(signalSize)), "setSliceAndDice")
+
+
+def error_test(p: int, N: int, iters: int = 0, **opts) -> IterReport:
+    rep = IterReport()
+    o = default_opts(**opts)
+    _check(lib.gl_error_test(int(p), int(N), ctypes.byref(o), int(iters), ctypes.byref(rep)), "error_test")
+    return rep
+
+
+def probe_fp64_peak(device: int = 0, ms: float = 200.0) -> float:
+    t = ctypes.c_double()
+    _check(lib.gl_probe_fp64_peak(int(device), float(ms), ctypes.byref(t)), "probe_fp64_peak")
+    return t.value
+
+
+def describe(p: int, N: int, mode: int = MODE_FUSED, **opts) -> PlanInfo:
+    """The layout a plan for (p, N) would use; needs no GPU."""
+    info = PlanInfo()
+    o = default_opts(mode=mode, **opts)
+    _check(lib.gl_plan_describe(int(p), int(N), ctypes.byref(o), ctypes.byref(info)), f"describe p={p} N={N}")
+    return info
+
+
+def error_string(status: int) -> str:
+    return lib.gl_error_string(int(status)).decode()
+
+
+def version() -> int:
+    return int(lib.gl_version())

@@ -1,0 +1,80 @@
+"""Build libgpulucas_gb300.so in-tree with nvcc for sm_103a (no torch extension machinery).
+
+The translation units compile in parallel; the result lands beside this file and is
+what ``gpulucas_gb300`` loads.  Host code is compiled with -ffp-contract=off so the
+double-double tables are bit-identical on x86_64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libgpulucas_gb300.so")
+HOSTCHECK = os.path.join(HERE, "libgl_hostcheck.so")
+
+SOURCES = ["gl_kernels.cu", "gl_capi.cpp", "gl_tables.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def common_flags() -> list[str]:
+    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall",
+            "-I", os.path.join(HERE, "..", "include")] + ARCH
+
+
+def _compile(src: str, verbose_ptxas: bool) -> str:
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc()] + common_flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
+    if src.endswith(".cu"):
+        cmd = [nvcc(), "-x", "cu"] + common_flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose_ptxas:
+            cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    if verbose_ptxas and r.stderr:
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build(verbose_ptxas: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_hostcheck() -> str:
+    """Host-only build of the device arithmetic helpers, for the CPU test suite."""
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = HOSTCHECK + ".tmp"
+    cmd = [nvcc(), "-x", "cu", "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           os.path.join(CSRC, "gl_hostcheck.cu"), os.path.join(CSRC, "gl_tables.cpp"), "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"hostcheck build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, HOSTCHECK)
+    return HOSTCHECK
+
+
+if __name__ == "__main__":
+    print(build(verbose_ptxas="-v" in sys.argv))
+    print(build_hostcheck())

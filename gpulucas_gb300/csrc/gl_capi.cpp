@@ -1,0 +1,697 @@
+// gl_capi.cpp -- the C ABI (include/gpulucas.h): plans, iteration, residues and the
+// reference-named entry points errorTest / mersenneTest / setSliceAndDice.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gl_internal.h"
+#include "gl_tables.h"
+
+using namespace gl;
+
+struct gl_plan {
+  int p = 0, N = 0, M = 0, LO = 0, n = 0;
+  int mode = GL_MODE_FUSED, device = 0;
+  double error_limit = 0.4;
+  int check_every = 1000;
+  int use_graphs = 1;
+  cudaStream_t stream = nullptr;
+  FusedGeom fg{};
+  PlainGeom pg{};
+  IterArgs args{};
+  std::vector<void*> allocs;
+  Status* h_status = nullptr;  // pinned
+  int64_t iters_done = 0;
+  double run_maxerr = 0.0;
+  bool from_state = false;     // next fused iteration loads (digit, hi)
+  bool carry_valid = true;     // device (digit, hi) matches the current products
+  cudaGraphExec_t gexec = nullptr;
+  int gexec_iters = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  size_t device_bytes = 0;
+};
+
+namespace {
+
+constexpr int kGraphBatch = 64;
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? GL_OK : GL_ERR_CUDA; }
+
+#define GL_CUDA(call)                                \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return GL_ERR_CUDA;       \
+  } while (0)
+
+template <typename T>
+int dev_alloc(gl_plan* pl, T** ptr, size_t count) {
+  void* p = nullptr;
+  size_t bytes = sizeof(T) * count;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return GL_ERR_NOMEM;
+  pl->allocs.push_back(p);
+  pl->device_bytes += bytes;
+  *ptr = static_cast<T*>(p);
+  return GL_OK;
+}
+
+bool fill_line_plan(int L, LinePlan* lp) {
+  std::vector<int> r = radix_plan(L, 16);
+  if (r.empty() || r.size() > 8) return false;
+  lp->L = L;
+  lp->nst = (int)r.size();
+  for (int i = 0; i < 8; ++i) lp->radix[i] = i < lp->nst ? r[i] : 0;
+  return true;
+}
+
+int round_up32(int x) { return (x + 31) / 32 * 32; }
+
+// Pick M = W * H: both must factor into radices <= 16 and {3,5,7}; prefer H near
+// sqrt(M) and a power of two; two double-buffered rows must fit one CTA (W <= 3072).
+int choose_fused_geom(int M, int force_h, int force_g, FusedGeom* g) {
+  int bestH = 0;
+  double best = 1e30;
+  const double target = std::log2((double)M) / 2.0;
+  for (int H = 2; H <= M / 2; ++H) {
+    if (M % H) continue;
+    if (force_h && H != force_h) continue;
+    const int W = M / H;
+    if (W > 3072 || H > 3072) continue;
+    LinePlan a, b;
+    if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
+    double cost = std::fabs(std::log2((double)H) - target);
+    if (H & (H - 1)) cost += 0.75;  // odd factors in the column length
+    if (H & 1) cost += 2.0;
+    if (cost < best) {
+      best = cost;
+      bestH = H;
+    }
+  }
+  if (!bestH) return GL_ERR_SIZE;
+  g->H = bestH;
+  g->W = M / bestH;
+  fill_line_plan(g->W, &g->pw);
+  fill_line_plan(g->H, &g->ph);
+  // columns per CTA: two shared buffers of G*H complex, at most 96 KiB when possible
+  int G = 1;
+  if (force_g) {
+    if (g->W % force_g) return GL_ERR_ARG;
+    G = force_g;
+  } else {
+    for (int c = 1; c <= 64 && c <= g->W; ++c)
+      if (g->W % c == 0 && (size_t)c * g->H * 32 <= 96 * 1024) G = c;
+  }
+  g->G = G;
+  g->sm_col = (size_t)2 * G * g->H * 16;
+  g->sm_row = (size_t)2 * 2 * g->W * 16;
+  if (g->sm_col > 200 * 1024 || g->sm_row > 200 * 1024) return GL_ERR_SIZE;
+  auto threads = [](int points) {
+    int t = round_up32((points + 15) / 16);
+    return t < 64 ? 64 : (t > kMaxThreads ? kMaxThreads : t);
+  };
+  g->t_col = threads(G * g->H);
+  g->t_row = threads(2 * g->W);
+  return GL_OK;
+}
+
+int choose_plain_geom(int M, PlainGeom* g) {
+  std::vector<int> r = radix_plan(M, 4);
+  if (r.empty() || r.size() > 40) return GL_ERR_SIZE;
+  g->nst = (int)r.size();
+  for (int i = 0; i < g->nst; ++i) g->radix[i] = r[i];
+  g->threads = 256;
+  return GL_OK;
+}
+
+void free_plan(gl_plan* pl) {
+  if (!pl) return;
+  if (pl->device >= 0) cudaSetDevice(pl->device);
+  if (pl->gexec) cudaGraphExecDestroy(pl->gexec);
+  for (void* p : pl->allocs) cudaFree(p);
+  if (pl->h_status) cudaFreeHost(pl->h_status);
+  if (pl->ev0) cudaEventDestroy(pl->ev0);
+  if (pl->ev1) cudaEventDestroy(pl->ev1);
+  if (pl->stream) cudaStreamDestroy(pl->stream);
+  delete pl;
+}
+
+int launch_iterations(gl_plan* pl, int64_t k) {
+  for (int64_t i = 0; i < k; ++i) {
+    cudaError_t e;
+    if (pl->mode == GL_MODE_PLAIN) {
+      e = launch_plain_iteration(pl->args, pl->pg, pl->stream);
+    } else {
+      e = launch_fused_iteration(pl->args, pl->fg, pl->stream, pl->from_state);
+      pl->from_state = false;
+    }
+    if (e != cudaSuccess) return GL_ERR_CUDA;
+  }
+  return GL_OK;
+}
+
+// Enqueue k iterations, with batches of kGraphBatch replayed from one CUDA graph.
+int enqueue(gl_plan* pl, int64_t k) {
+  if (k <= 0) return GL_OK;
+  int rc;
+  if (pl->from_state) {  // the state-loading first pass is never captured
+    if ((rc = launch_iterations(pl, 1)) != GL_OK) return rc;
+    --k;
+  }
+  if (pl->use_graphs && k >= kGraphBatch) {
+    if (!pl->gexec) {
+      cudaGraph_t graph = nullptr;
+      GL_CUDA(cudaStreamBeginCapture(pl->stream, cudaStreamCaptureModeThreadLocal));
+      int lrc = launch_iterations(pl, kGraphBatch);
+      cudaError_t ec = cudaStreamEndCapture(pl->stream, &graph);
+      if (lrc != GL_OK || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return GL_ERR_CUDA;
+      }
+      cudaError_t ei = cudaGraphInstantiate(&pl->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        pl->gexec = nullptr;
+        return GL_ERR_CUDA;
+      }
+      pl->gexec_iters = kGraphBatch;
+    }
+    while (k >= pl->gexec_iters) {
+      GL_CUDA(cudaGraphLaunch(pl->gexec, pl->stream));
+      k -= pl->gexec_iters;
+    }
+  }
+  return launch_iterations(pl, k);
+}
+
+// Wait for the stream and fold the device status into the plan.
+int read_status(gl_plan* pl, double* maxerr_out) {
+  GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
+  if (e > pl->run_maxerr) pl->run_maxerr = e;
+  if (maxerr_out) *maxerr_out = e;
+  if (pl->h_status->flags) return GL_ERR_OVERFLOW;
+  if (e >= pl->error_limit) return GL_ERR_ROUNDOFF;
+  return GL_OK;
+}
+
+// Host side of addPseudoBalanced + rebalanceIrrIntSEQGPU (IrrBaseBalanced.cu:117-169):
+// one balanced carry pass with the final carry wrapped into word 0.
+void rebalance_host(const gl_plan* pl, const std::vector<int32_t>& bits, const int32_t* digit, const int8_t* hi,
+                    int32_t* out) {
+  const int N = pl->N;
+  for (int j = 0; j < N; ++j) out[j] = digit[j] + hi[j == 0 ? N - 1 : j - 1];
+  int carry = 0;
+  for (int j = 0; j < N; ++j) {
+    const int base = 1 << bits[j], half = base >> 1;
+    const int t = out[j] + carry;
+    if (t >= half) { out[j] = t - base; carry = 1; }
+    else if (t < -half) { out[j] = t + base; carry = -1; }
+    else { out[j] = t; carry = 0; }
+  }
+  if (carry) out[0] += carry;
+}
+
+// Canonical non-negative digits of the value mod 2^p - 1 (floor carries, the carry
+// out of the top word re-enters at word 0 since 2^p == 1), then the low 64 bits
+// (print_residue, gpuLucas.cu:1288-1352).  Returns 1 if the value is 0 mod 2^p - 1.
+int residue_host(const gl_plan* pl, const std::vector<int32_t>& bits, const int32_t* balanced, uint64_t* res64) {
+  const int N = pl->N;
+  std::vector<int64_t> d(balanced, balanced + N);
+  for (int pass = 0; pass < 8; ++pass) {
+    int64_t carry = 0;
+    for (int j = 0; j < N; ++j) {
+      const int64_t base = (int64_t)1 << bits[j];
+      int64_t v = d[j] + carry;
+      int64_t q = v >= 0 ? v >> bits[j] : -((-v + base - 1) >> bits[j]);
+      d[j] = v - q * base;
+      carry = q;
+    }
+    if (carry == 0) break;
+    d[0] += carry;
+  }
+  bool all0 = true, allmax = true;
+  for (int j = 0; j < N; ++j) {
+    if (d[j] != 0) all0 = false;
+    if (d[j] != ((int64_t)1 << bits[j]) - 1) allmax = false;
+  }
+  uint64_t r = 0;
+  int pos = 0;
+  for (int j = 0; j < N && pos < 64; ++j) {
+    r |= (uint64_t)d[j] << pos;  // bits above 64 fall off
+    pos += bits[j];
+  }
+  if (allmax) r = 0;
+  *res64 = r;
+  return (all0 || allmax) ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gl_version(void) { return 100; }
+
+const char* gl_error_string(int s) {
+  switch (s) {
+    case GL_OK: return "ok";
+    case GL_ERR_ARG: return "bad argument";
+    case GL_ERR_RATIO: return "p/N outside the carry-depth table (ratio >= 22)";
+    case GL_ERR_SIZE: return "N must be even with N/2 = 2^a 3^b 5^c 7^d and a usable FFT layout";
+    case GL_ERR_CUDA: return "CUDA runtime error";
+    case GL_ERR_NOMEM: return "out of memory";
+    case GL_ERR_ROUNDOFF: return "round-off error reached the limit";
+    case GL_ERR_OVERFLOW: return "product out of the exactly representable / sliced range";
+    case GL_ERR_NODEVICE: return "no CUDA device";
+    case GL_ERR_IO: return "checkpoint I/O error";
+    case GL_ERR_CHECKPOINT: return "checkpoint does not match the test";
+    case GL_ERR_STATE: return "call not valid in this state";
+    default: return "unknown status";
+  }
+}
+
+int gl_default_opts(gl_plan_opts* o) {
+  if (!o) return GL_ERR_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->mode = GL_MODE_FUSED;
+  o->device = 0;
+  o->error_limit = 0.4;
+  o->check_every = 1000;
+  o->use_graphs = 1;
+  return GL_OK;
+}
+
+int setSliceAndDice(int testPrime, int signalSize) {
+  if (testPrime <= 2 || signalSize <= 0) return GL_ERR_ARG;
+  int n = slice_depth(testPrime, signalSize);
+  return n < 0 ? GL_ERR_RATIO : n;
+}
+
+int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
+  if (!out) return GL_ERR_ARG;
+  *out = nullptr;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  if (p < 3 || N < 16 || (N & 1) || N > p) return GL_ERR_ARG;
+  if (o.mode != GL_MODE_FUSED && o.mode != GL_MODE_PLAIN) return GL_ERR_ARG;
+  if (!(o.error_limit > 0.0 && o.error_limit <= 0.5) || o.check_every < 1) return GL_ERR_ARG;
+  const int n = slice_depth(p, N);
+  if (n < 0) return GL_ERR_RATIO;
+  const int M = N / 2;
+  FusedGeom fg{};
+  PlainGeom pg{};
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, o.fft_h, o.cols_per_cta, &fg) : choose_plain_geom(M, &pg);
+  if (rc != GL_OK) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GL_ERR_NODEVICE;
+  if (o.device < 0 || o.device >= ndev) return GL_ERR_ARG;
+  if (cudaSetDevice(o.device) != cudaSuccess) return GL_ERR_CUDA;
+
+  gl_plan* pl = new (std::nothrow) gl_plan();
+  if (!pl) return GL_ERR_NOMEM;
+  pl->p = p; pl->N = N; pl->M = M; pl->LO = p / N; pl->n = n;
+  pl->mode = o.mode; pl->device = o.device;
+  pl->error_limit = o.error_limit; pl->check_every = o.check_every; pl->use_graphs = o.use_graphs;
+  pl->fg = fg; pl->pg = pg;
+
+#define GL_TRY(x)             \
+  do {                        \
+    int r_ = (x);             \
+    if (r_ != GL_OK) {        \
+      free_plan(pl);          \
+      return r_;              \
+    }                         \
+  } while (0)
+#define GL_TRYC(x) GL_TRY(cuda_status(x))
+
+  GL_TRYC(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+  GL_TRYC(cudaEventCreate(&pl->ev0));
+  GL_TRYC(cudaEventCreate(&pl->ev1));
+  GL_TRYC(cudaMallocHost((void**)&pl->h_status, sizeof(Status)));
+
+  std::vector<int32_t> bits;
+  std::vector<uint8_t> flags;
+  std::vector<double> A, Ainv;
+  std::vector<HostCplx> twM, twW, twH;
+  word_tables(p, N, bits, flags);
+  weight_tables(p, N, 2.0 * N, A, Ainv);
+  twiddle_table(M, twM);
+
+  IterArgs& a = pl->args;
+  a.N = N; a.M = M; a.LO = pl->LO; a.n = n;
+  long long* ll;
+  unsigned char* fl;
+  double *dA, *dAi;
+  DevCplx *Z, *Z2 = nullptr, *dtwM, *dtwW = nullptr, *dtwH = nullptr;
+  int* digit;
+  signed char* hi;
+  Status* status;
+  GL_TRY(dev_alloc(pl, &ll, N));
+  GL_TRY(dev_alloc(pl, &fl, N));
+  GL_TRY(dev_alloc(pl, &dA, N));
+  GL_TRY(dev_alloc(pl, &dAi, N));
+  GL_TRY(dev_alloc(pl, &Z, M));
+  GL_TRY(dev_alloc(pl, &dtwM, M));
+  GL_TRY(dev_alloc(pl, &digit, N));
+  GL_TRY(dev_alloc(pl, &hi, N));
+  GL_TRY(dev_alloc(pl, &status, 1));
+  if (o.mode == GL_MODE_PLAIN) GL_TRY(dev_alloc(pl, &Z2, M));
+  if (o.mode == GL_MODE_FUSED) {
+    twiddle_table(fg.W, twW);
+    twiddle_table(fg.H, twH);
+    GL_TRY(dev_alloc(pl, &dtwW, fg.W));
+    GL_TRY(dev_alloc(pl, &dtwH, fg.H));
+    GL_TRYC(cudaMemcpy(dtwW, twW.data(), sizeof(DevCplx) * fg.W, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dtwH, twH.data(), sizeof(DevCplx) * fg.H, cudaMemcpyHostToDevice));
+    a.W = fg.W; a.H = fg.H; a.G = fg.G; a.pw = fg.pw; a.ph = fg.ph;
+    GL_TRYC(set_fused_smem_limits(fg));
+  }
+  GL_TRYC(cudaMemcpy(fl, flags.data(), N, cudaMemcpyHostToDevice));
+  GL_TRYC(cudaMemcpy(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  GL_TRYC(cudaMemcpy(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  GL_TRYC(cudaMemcpy(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+  a.ll = ll; a.flags = fl; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;
+  a.twM = dtwM; a.twW = dtwW; a.twH = dtwH; a.digit = digit; a.hi = hi; a.status = status;
+  *out = pl;
+  int r = gl_reset(pl);
+  if (r != GL_OK) {
+    free_plan(pl);
+    *out = nullptr;
+    return r;
+  }
+  return GL_OK;
+#undef GL_TRY
+#undef GL_TRYC
+}
+
+int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info) {
+  if (!info) return GL_ERR_ARG;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  if (p < 3 || N < 16 || (N & 1) || N > p) return GL_ERR_ARG;
+  if (o.mode != GL_MODE_FUSED && o.mode != GL_MODE_PLAIN) return GL_ERR_ARG;
+  const int n = slice_depth(p, N);
+  if (n < 0) return GL_ERR_RATIO;
+  gl_plan tmp;
+  tmp.p = p; tmp.N = N; tmp.M = N / 2; tmp.LO = p / N; tmp.n = n; tmp.mode = o.mode;
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, o.cols_per_cta, &tmp.fg)
+                                   : choose_plain_geom(tmp.M, &tmp.pg);
+  if (rc != GL_OK) return rc;
+  tmp.device = -1;
+  int r = gl_plan_get_info(&tmp, info);
+  if (o.mode == GL_MODE_FUSED) {
+    const size_t M = tmp.M, N8 = (size_t)N * 8;
+    info->device_bytes = N8 /*ll*/ + N /*flags*/ + 2 * N8 /*A, Ainv*/ + 2 * M * 16 /*Z, twM*/ +
+                         (size_t)(tmp.fg.W + tmp.fg.H) * 16 + (size_t)N * 5 + 16;
+  }
+  return r;
+}
+
+int gl_plan_destroy(gl_plan* plan) {
+  if (!plan) return GL_ERR_ARG;
+  free_plan(plan);
+  return GL_OK;
+}
+
+int gl_plan_get_info(const gl_plan* pl, gl_plan_info* info) {
+  if (!pl || !info) return GL_ERR_ARG;
+  std::memset(info, 0, sizeof(*info));
+  info->p = pl->p; info->N = pl->N;
+  info->lo_bits = pl->LO; info->hi_bits = pl->LO + 1;
+  info->carry_depth = pl->n; info->mode = pl->mode;
+  if (pl->mode == GL_MODE_FUSED) {
+    info->fft_w = pl->fg.W; info->fft_h = pl->fg.H; info->cols_per_cta = pl->fg.G;
+    for (int i = 0; i < pl->fg.pw.nst; ++i) info->radix_w[i] = pl->fg.pw.radix[i];
+    for (int i = 0; i < pl->fg.ph.nst; ++i) info->radix_h[i] = pl->fg.ph.radix[i];
+    info->threads_col = pl->fg.t_col; info->threads_row = pl->fg.t_row;
+    info->smem_col = (int)pl->fg.sm_col; info->smem_row = (int)pl->fg.sm_row;
+  } else {
+    info->fft_w = pl->M; info->fft_h = 1;
+    for (int i = 0; i < pl->pg.nst && i < 8; ++i) info->radix_w[i] = pl->pg.radix[i];
+  }
+  info->device_bytes = pl->device_bytes;
+  return GL_OK;
+}
+
+int gl_reset(gl_plan* pl) {
+  if (!pl) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  GL_CUDA(launch_set_initial(pl->args, pl->mode, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  pl->iters_done = 0;
+  pl->run_maxerr = 0.0;
+  pl->from_state = false;
+  pl->carry_valid = true;
+  return GL_OK;
+}
+
+int gl_iterate(gl_plan* pl, int64_t iters, gl_iter_report* rep) {
+  if (!pl || iters < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  double call_max = 0.0;
+  int status = GL_OK;
+  int64_t done = 0;
+  GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
+  if (pl->mode == GL_MODE_PLAIN && !pl->carry_valid && iters > 0) {
+    GL_CUDA(launch_dice(pl->args, pl->stream));
+    pl->carry_valid = true;
+  }
+  while (done < iters) {
+    const int64_t b = iters - done < pl->check_every ? iters - done : pl->check_every;
+    int rc = enqueue(pl, b);
+    if (rc != GL_OK) return rc;
+    done += b;
+    pl->iters_done += b;
+    pl->carry_valid = pl->mode == GL_MODE_PLAIN;
+    double e = 0.0;
+    status = read_status(pl, &e);
+    if (status == GL_ERR_CUDA) return status;
+    if (e > call_max) call_max = e;
+    if (status != GL_OK) break;
+  }
+  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
+  GL_CUDA(cudaEventSynchronize(pl->ev1));
+  float ms = 0.f;
+  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
+  if (rep) {
+    rep->iterations = done;
+    rep->total_iterations = pl->iters_done;
+    rep->max_roundoff = call_max;
+    rep->ms = ms;
+    rep->status = status;
+  }
+  return status;
+}
+
+int gl_plan_stream(gl_plan* pl, void** cuda_stream) {
+  if (!pl || !cuda_stream) return GL_ERR_ARG;
+  *cuda_stream = (void*)pl->stream;
+  return GL_OK;
+}
+
+int gl_enqueue(gl_plan* pl, int64_t iters) {
+  if (!pl || iters < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  if (pl->mode == GL_MODE_PLAIN && !pl->carry_valid && iters > 0) {
+    GL_CUDA(launch_dice(pl->args, pl->stream));
+    pl->carry_valid = true;
+  }
+  int rc = enqueue(pl, iters);
+  if (rc != GL_OK) return rc;
+  pl->iters_done += iters;
+  if (iters > 0) pl->carry_valid = pl->mode == GL_MODE_PLAIN;
+  return GL_OK;
+}
+
+int gl_sync_status(gl_plan* pl, gl_iter_report* rep) {
+  if (!pl) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  double e = 0.0;
+  int st = read_status(pl, &e);
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    rep->total_iterations = pl->iters_done;
+    rep->max_roundoff = e;
+    rep->status = st;
+  }
+  return st;
+}
+
+int gl_launches_per_iteration(const gl_plan* pl) {
+  if (!pl) return GL_ERR_ARG;
+  if (pl->mode == GL_MODE_FUSED) return 3;
+  return 2 * pl->pg.nst + 4;
+}
+
+int gl_get_products(gl_plan* pl, int64_t* ll_out) {
+  if (!pl || !ll_out) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  GL_CUDA(cudaMemcpyAsync(ll_out, pl->args.ll, sizeof(int64_t) * pl->N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  return GL_OK;
+}
+
+static int ensure_carry(gl_plan* pl) {
+  if (!pl->carry_valid) {
+    GL_CUDA(launch_dice(pl->args, pl->stream));
+    pl->carry_valid = true;
+  }
+  return GL_OK;
+}
+
+int gl_get_carry_state(gl_plan* pl, int32_t* digit_out, int8_t* hi_out) {
+  if (!pl || !digit_out || !hi_out) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  int rc = ensure_carry(pl);
+  if (rc != GL_OK) return rc;
+  GL_CUDA(cudaMemcpyAsync(digit_out, pl->args.digit, sizeof(int32_t) * pl->N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(hi_out, pl->args.hi, pl->N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  return GL_OK;
+}
+
+int gl_set_products(gl_plan* pl, const int64_t* ll, int64_t iterations) {
+  if (!pl || !ll || iterations < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  GL_CUDA(cudaMemcpyAsync(pl->args.ll, ll, sizeof(int64_t) * pl->N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  pl->iters_done = iterations;
+  pl->from_state = false;
+  pl->carry_valid = false;
+  return GL_OK;
+}
+
+int gl_set_carry_state(gl_plan* pl, const int32_t* digit, const int8_t* hi, int64_t iterations) {
+  if (!pl || !digit || !hi || iterations < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  GL_CUDA(cudaMemcpyAsync(pl->args.digit, digit, sizeof(int32_t) * pl->N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->args.hi, hi, pl->N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  pl->iters_done = iterations;
+  pl->from_state = pl->mode == GL_MODE_FUSED;
+  pl->carry_valid = true;
+  return GL_OK;
+}
+
+int gl_get_residue(gl_plan* pl, int32_t* digits_out, uint64_t* res64, int* is_zero) {
+  if (!pl) return GL_ERR_ARG;
+  std::vector<int32_t> digit(pl->N), out(pl->N), bits;
+  std::vector<int8_t> hi(pl->N);
+  std::vector<uint8_t> flags;
+  int rc = gl_get_carry_state(pl, digit.data(), hi.data());
+  if (rc != GL_OK) return rc;
+  word_tables(pl->p, pl->N, bits, flags);
+  rebalance_host(pl, bits, digit.data(), hi.data(), out.data());
+  if (digits_out) std::memcpy(digits_out, out.data(), sizeof(int32_t) * pl->N);
+  uint64_t r = 0;
+  int z = residue_host(pl, bits, out.data(), &r);
+  if (res64) *res64 = r;
+  if (is_zero) *is_zero = z;
+  return GL_OK;
+}
+
+int gl_mersenne_test(gl_plan* pl, int64_t iters, gl_result* res) {
+  if (!pl) return GL_ERR_ARG;
+  const bool full = iters == 0;
+  if (full) {
+    int rc = gl_reset(pl);
+    if (rc != GL_OK) return rc;
+    iters = (int64_t)pl->p - 2;
+  }
+  gl_iter_report rep{};
+  int st = gl_iterate(pl, iters, &rep);
+  if (st == GL_ERR_CUDA || st == GL_ERR_ARG) return st;
+  uint64_t r = 0;
+  int z = 0;
+  int rc = gl_get_residue(pl, nullptr, &r, &z);
+  if (rc != GL_OK) return rc;
+  if (res) {
+    res->p = pl->p;
+    res->N = pl->N;
+    res->iterations = pl->iters_done;
+    res->is_zero = z;
+    res->is_prime = (pl->iters_done == (int64_t)pl->p - 2 && z && st == GL_OK) ? 1 : 0;
+    res->res64 = r;
+    res->max_roundoff = pl->run_maxerr;
+    res->ms = rep.ms;
+  }
+  return st;
+}
+
+int gl_error_test(int p, int N, const gl_plan_opts* opts, int iters, gl_iter_report* rep) {
+  gl_plan* pl = nullptr;
+  int rc = gl_plan_create(p, N, opts, &pl);
+  if (rc != GL_OK) return rc;
+  if (iters <= 0) {
+    iters = p / 10000;
+    if (iters < 100) iters = 100;
+    if (iters > 2500) iters = 2500;
+  }
+  rc = gl_iterate(pl, iters, rep);
+  gl_plan_destroy(pl);
+  return rc;
+}
+
+float errorTest(int testPrime, int signalSize) {
+  gl_iter_report rep{};
+  int rc = gl_error_test(testPrime, signalSize, nullptr, 0, &rep);
+  if (rc != GL_OK || rep.iterations <= 0) return -1.0f;
+  return (float)(rep.ms / (double)rep.iterations);
+}
+
+int mersenneTest(int testPrime, int signalSize) {
+  gl_plan* pl = nullptr;
+  int rc = gl_plan_create(testPrime, signalSize, nullptr, &pl);
+  if (rc != GL_OK) return rc;
+  gl_result res{};
+  rc = gl_mersenne_test(pl, 0, &res);
+  gl_plan_destroy(pl);
+  if (rc != GL_OK) return rc;
+  if (res.is_prime)
+    std::printf("M( %d )P, n = %d, gpulucas_gb300 v%d.%d.%d\n", testPrime, signalSize, 0, 1, 0);
+  else
+    std::printf("M( %d )C, 0x%016llx, n = %d, gpulucas_gb300 v%d.%d.%d\n", testPrime,
+                (unsigned long long)res.res64, signalSize, 0, 1, 0);
+  std::fflush(stdout);
+  return res.is_prime;
+}
+
+int gl_probe_fp64_peak(int device, double ms, double* tflops) {
+  if (!tflops || ms <= 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(device));
+  int nsm = 0;
+  GL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  const int threads = 256, blocks = nsm * 4;
+  double* buf = nullptr;
+  GL_CUDA(cudaMalloc(&buf, sizeof(double) * threads * blocks));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  long long iters = 1024;
+  float el = 0.f;
+  int rc = GL_OK;
+  for (int rep = 0; rep < 12; ++rep) {
+    cudaEventRecord(a, 0);
+    if (probe_fp64(blocks, threads, iters, buf, 0) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
+    cudaEventRecord(b, 0);
+    if (cudaEventSynchronize(b) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
+    cudaEventElapsedTime(&el, a, b);
+    if (el >= ms) break;
+    iters *= 2;
+  }
+  if (rc == GL_OK) {
+    const double fmas = (double)blocks * threads * 8.0 * (double)iters;
+    *tflops = 2.0 * fmas / (el * 1e-3) / 1e12;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  return rc;
+}
+
+}  // extern "C"

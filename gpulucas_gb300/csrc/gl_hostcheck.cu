@@ -1,0 +1,88 @@
+// gl_hostcheck.cu -- the device arithmetic helpers (small DFTs, integer-domain
+// rounding and conversion, dicing) compiled for the host, so the CPU test suite can
+// check them against numpy and the oracle without a GPU.  Not used by the product.
+#include <cstdint>
+
+#include "gl_device.cuh"
+
+using namespace gl;
+
+template <int S>
+static void run_dft(int R, cplx* x) {
+  switch (R) {
+    case 2: dft<2, S>(x); break;
+    case 3: dft<3, S>(x); break;
+    case 4: dft<4, S>(x); break;
+    case 5: dft<5, S>(x); break;
+    case 7: dft<7, S>(x); break;
+    case 8: dft<8, S>(x); break;
+    case 16: dft<16, S>(x); break;
+    default: break;
+  }
+}
+
+extern "C" {
+
+// in-place DFT of R interleaved complex doubles; sign -1 forward, +1 inverse
+int hc_dft(int R, int sign, double* xy) {
+  if (R != 2 && R != 3 && R != 4 && R != 5 && R != 7 && R != 8 && R != 16) return -1;
+  cplx* x = reinterpret_cast<cplx*>(xy);
+  if (sign < 0) run_dft<-1>(R, x);
+  else run_dft<1>(R, x);
+  return 0;
+}
+
+long long hc_round(double x, unsigned long long* err64, int* big) {
+  *big = 0;
+  return round_ll_bits(x, err64, big);
+}
+
+double hc_dbl_from_int(int v) { return dbl_from_int(v); }
+
+// dice one word j from products ll (cyclic, length N) with flags
+long long hc_dice_sum(int LO, int n, unsigned f, const long long* ll, int N, int j) {
+  return dice_sum(LO, n, f, [&](int i) {
+    int k = j - i;
+    return ll[k < 0 ? k + N : k];
+  });
+}
+
+void hc_balanced_split(long long sum, int bits, int* digit, int* hi) { balanced_split(sum, bits, digit, hi); }
+
+}  // extern "C"
+
+// The product's host tables (gl_tables.cpp), for pinning against the golden values.
+#include <vector>
+
+#include "gl_tables.h"
+
+extern "C" {
+
+void hc_weights(int p, int N, double* A, double* Ainv) {
+  std::vector<double> a, ai;
+  gl::weight_tables(p, N, (double)N, a, ai);
+  for (int j = 0; j < N; ++j) {
+    A[j] = a[j];
+    Ainv[j] = ai[j];
+  }
+}
+
+void hc_twiddles(int L, double* re, double* im) {
+  for (int t = 0; t < L; ++t) {
+    gl::HostCplx w = gl::twiddle(t, L);
+    re[t] = w.re;
+    im[t] = w.im;
+  }
+}
+
+void hc_word_tables(int p, int N, int* bits, unsigned char* flags) {
+  std::vector<int32_t> b;
+  std::vector<uint8_t> f;
+  gl::word_tables(p, N, b, f);
+  for (int j = 0; j < N; ++j) {
+    bits[j] = b[j];
+    flags[j] = f[j];
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// gl_internal.h -- plan layout and kernel launch interface (not part of the C ABI).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gpulucas.h"
+
+namespace gl {
+
+// the fused kernels are compiled for at most this many threads per CTA
+constexpr int kMaxThreads = 512;
+
+struct DevCplx {
+  double re, im;
+};
+
+// Stockham radix sequence of one line DFT of length L (first stage first).
+struct LinePlan {
+  int L;
+  int nst;
+  int radix[8];
+};
+
+// Round-off / range status written by the kernels, read by the host between batches.
+struct Status {
+  unsigned long long maxerr64;  // max |x - rint(x)| * 2^64 over the batch
+  unsigned int flags;           // kStatusBig | kStatusSlice
+  unsigned int pad;
+};
+constexpr unsigned kStatusBig = 1u;    // |product| >= 2^51: doubles cannot hold it exactly
+constexpr unsigned kStatusSlice = 2u;  // product bits beyond what n+1 slices place
+
+// Geometry of the fused form: the N/2 complex points are an H x W array
+// (row-major, element m = m1 + W*m2); column passes take G columns per CTA.
+struct FusedGeom {
+  int W, H, G;
+  int t_col, t_row;          // threads per CTA
+  size_t sm_col, sm_row;     // dynamic shared memory bytes
+  LinePlan pw, ph;
+};
+
+struct PlainGeom {
+  int nst;
+  int radix[40];
+  int threads;
+};
+
+// Arguments of one iteration (passed by value to every kernel).
+struct IterArgs {
+  int N, M, W, H, G, LO, n;
+  long long* ll;              // loop-carried products, N int64 (fused)
+  const unsigned char* flags; // bitsPerWord8, N
+  const double* A;            // N weights
+  const double* Ainv;         // N inverse weights with 1/(2N) folded in
+  DevCplx* Z;                 // M complex work array [H][W]
+  DevCplx* Z2;                // M complex (plain: ping-pong)
+  const DevCplx* twM;         // exp(-2 pi i t/M), t < M
+  const DevCplx* twW;         // exp(-2 pi i t/W), t < W
+  const DevCplx* twH;         // exp(-2 pi i t/H), t < H
+  int* digit;                 // plain: i_signal, N
+  signed char* hi;            // plain: i_hiBitArr, N
+  Status* status;
+  LinePlan pw, ph;
+};
+
+// launchers (gl_kernels.cu); all asynchronous on `s`
+// from_state: the first column pass loads the carry-save state (digit, hi) instead of
+// dicing the products, exactly as loadIntToDoubleIBDWT (gpuLucas.cu:730-766) does
+cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state);
+cudaError_t launch_plain_iteration(const IterArgs& a, const PlainGeom& g, cudaStream_t s);
+cudaError_t launch_set_initial(const IterArgs& a, int mode, cudaStream_t s);
+// carry-save state (digit, hi) = dice(ll) for the fused form; plain keeps it already
+cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
+cudaError_t set_fused_smem_limits(const FusedGeom& g);
+cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s);
+
+}  // namespace gl

@@ -1,0 +1,194 @@
+// gl_tables.cpp -- word sizes, weights and twiddles for one Lucas-Lehmer test.
+//
+// Double-double arithmetic after Dekker (1971) and Knuth (TAOCP 4.2.2): two-sum,
+// two-product through fma, and renormalisation; the same published algorithms the
+// QD library implements, which the reference uses for its weights
+// (gpuLucas.cu:673-686).  exp() is a Taylor series on x/2^10 followed by ten
+// squarings carried on expm1; sin/cos are Taylor series after an exact reduction to
+// one octant by integer arithmetic on the angle's numerator.
+#include "gl_tables.h"
+
+#include <cmath>
+
+namespace gl {
+namespace {
+
+struct DD {
+  double hi, lo;
+};
+
+inline DD quick_two_sum(double a, double b) {
+  double s = a + b;
+  return {s, b - (s - a)};
+}
+inline DD two_sum(double a, double b) {
+  double s = a + b;
+  double bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+inline DD two_prod(double a, double b) {
+  double p = a * b;
+  return {p, std::fma(a, b, -p)};
+}
+inline DD dd(double a) { return {a, 0.0}; }
+inline DD operator+(DD a, DD b) {
+  DD s = two_sum(a.hi, b.hi);
+  DD t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+inline DD operator-(DD a) { return {-a.hi, -a.lo}; }
+inline DD operator-(DD a, DD b) { return a + (-b); }
+inline DD operator*(DD a, DD b) {
+  DD p = two_prod(a.hi, b.hi);
+  p.lo += a.hi * b.lo;
+  p.lo += a.lo * b.hi;
+  return quick_two_sum(p.hi, p.lo);
+}
+inline DD mul_d(DD a, double b) {
+  DD p = two_prod(a.hi, b);
+  p.lo += a.lo * b;
+  return quick_two_sum(p.hi, p.lo);
+}
+inline DD operator/(DD a, DD b) {
+  double q1 = a.hi / b.hi;
+  DD r = a - mul_d(b, q1);
+  double q2 = r.hi / b.hi;
+  r = r - mul_d(b, q2);
+  double q3 = r.hi / b.hi;
+  return quick_two_sum(q1, q2) + dd(q3);
+}
+inline double to_double(DD a) { return a.hi + a.lo; }
+
+const DD kLn2 = {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
+const DD kPi4 = {0x1.921fb54442d18p-1, 0x1.1a62633145c07p-55};
+
+// exp(x), 0 <= x < 1
+DD exp_small(DD x) {
+  DD y = {std::ldexp(x.hi, -10), std::ldexp(x.lo, -10)};
+  DD term = y, sum = y;
+  for (int k = 2; k <= 14; ++k) {
+    term = (term * y) / dd((double)k);
+    sum = sum + term;
+  }
+  for (int i = 0; i < 10; ++i) {
+    DD two_s = {2.0 * sum.hi, 2.0 * sum.lo};
+    sum = two_s + sum * sum;
+  }
+  return dd(1.0) + sum;
+}
+
+// sin, cos of (pi/4) num/den, 0 <= num <= den
+void sincos_octant(int64_t num, int64_t den, DD* s, DD* c) {
+  DD x = kPi4 * (dd((double)num) / dd((double)den));
+  DD x2 = x * x;
+  DD st = x, ss = x, ct = dd(1.0), cs = dd(1.0);
+  for (int k = 1; k <= 14; ++k) {
+    st = -((st * x2) / dd((double)((2 * k) * (2 * k + 1))));
+    ss = ss + st;
+    ct = -((ct * x2) / dd((double)((2 * k - 1) * (2 * k))));
+    cs = cs + ct;
+  }
+  *s = ss;
+  *c = cs;
+}
+
+inline int64_t ceil_div_pos(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+int slice_depth(int p, int N) {
+  if (N <= 0) return -1;
+  int ratio = p / N;
+  if (ratio >= 22) return -1;
+  if (ratio >= 18) return 2;
+  if (ratio >= 16) return 3;
+  if (ratio >= 14) return 4;
+  if (ratio >= 12) return 5;
+  return 6;
+}
+
+void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>& flags) {
+  const int LO = p / N;
+  bits.resize(N);
+  flags.resize(N);
+  for (int j = 0; j < N; ++j)
+    bits[j] = (int32_t)(ceil_div_pos((int64_t)p * (j + 1), N) - ceil_div_pos((int64_t)p * j, N));
+  for (int j = 0; j < N; ++j) {
+    uint8_t v = 0;
+    for (int b = 0; b < 8; ++b) {
+      int k = ((j - b) % N + N) % N;
+      v |= (uint8_t)((bits[k] != LO ? 1 : 0) << b);
+    }
+    flags[j] = v;
+  }
+}
+
+void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, std::vector<double>& Ainv) {
+  A.resize(N);
+  Ainv.resize(N);
+  const DD dN = dd((double)N);
+  const DD den = dd(inv_scale_den);
+  for (int j = 0; j < N; ++j) {
+    // ceil(jp/N) - jp/N = r/N with r = ceil(jp/N)*N - jp, an exact integer
+    int64_t r = ceil_div_pos((int64_t)p * j, N) * N - (int64_t)p * j;
+    DD e = exp_small((dd((double)r) / dN) * kLn2);
+    A[j] = to_double(e);
+    Ainv[j] = to_double((dd(1.0) / e) / den);
+  }
+}
+
+HostCplx twiddle(int64_t t, int64_t L) {
+  t %= L;
+  if (t < 0) t += L;
+  int64_t u = 8 * t;
+  int64_t o = u / L;
+  int64_t r = u - o * L;
+  DD s, c;
+  if (o & 1) sincos_octant(L - r, L, &s, &c);
+  else sincos_octant(r, L, &s, &c);
+  double cs = to_double(c), sn = to_double(s), C, S;
+  switch (o) {
+    case 0: C = cs; S = sn; break;
+    case 1: C = sn; S = cs; break;
+    case 2: C = -sn; S = cs; break;
+    case 3: C = -cs; S = sn; break;
+    case 4: C = -cs; S = -sn; break;
+    case 5: C = -sn; S = -cs; break;
+    case 6: C = sn; S = -cs; break;
+    default: C = cs; S = -sn; break;
+  }
+  return {C, -S};
+}
+
+void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
+  tw.resize(L);
+  for (int64_t t = 0; t < L; ++t) tw[t] = twiddle(t, L);
+}
+
+std::vector<int> radix_plan(int n, int max_radix) {
+  std::vector<int> r;
+  if (n <= 0) return r;
+  int m = n;
+  const int pow2[4] = {16, 8, 4, 2};
+  for (int q : pow2) {
+    if (q > max_radix) continue;
+    while (m % q == 0) {
+      r.push_back(q);
+      m /= q;
+    }
+  }
+  const int odd[3] = {3, 5, 7};
+  for (int q : odd) {
+    while (m % q == 0) {
+      r.push_back(q);
+      m /= q;
+    }
+  }
+  if (m != 1) r.clear();
+  return r;
+}
+
+}  // namespace gl

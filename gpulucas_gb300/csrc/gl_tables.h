@@ -1,0 +1,35 @@
+// gl_tables.h -- host precompute of a test's word sizes, IBDWT weights and FFT
+// twiddles.  All floating point here is IEEE double / double-double with explicit
+// fma and -ffp-contract=off, so the tables are bit-identical on x86_64 and aarch64.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace gl {
+
+struct HostCplx {
+  double re, im;
+};
+
+// setSliceAndDice (gpuLucas.cu:323-343) extended to ratio 21; -1 when refused.
+int slice_depth(int p, int N);
+
+// bits[j] = ceil(p(j+1)/N) - ceil(pj/N) (computeBitsPerWord, gpuLucas.cu:688-694, in
+// exact integer arithmetic); flags[j] bit i = word (j-i) mod N has LO+1 bits, i < 8
+// (computeBitsPerWordVectors, gpuLucas.cu:700-714).
+void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>& flags);
+
+// A[j] = 2^(ceil(jp/N) - jp/N) and Ainv[j] = 2^-(ceil(jp/N) - jp/N) * scale, computed in
+// double-double and rounded once (computeWeightVectors, gpuLucas.cu:673-686, uses
+// scale = 1/N; the fused kernels need 1/(2N)).
+void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, std::vector<double>& Ainv);
+
+// exp(-2 pi i t / L) for t in [0, L), correctly rounded from double-double.
+void twiddle_table(int64_t L, std::vector<HostCplx>& tw);
+HostCplx twiddle(int64_t t, int64_t L);
+
+// factor n into the allowed radices (16, 8, 4, 2, 3, 5, 7), largest first; empty if
+// n has another prime factor.
+std::vector<int> radix_plan(int n, int max_radix);
+
+}  // namespace gl

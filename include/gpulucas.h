@@ -1,0 +1,158 @@
+/*
+ * gpulucas.h -- C ABI of gpulucas_gb300, a GB300-native Lucas-Lehmer engine for
+ * Mersenne numbers 2^p - 1 (irrational-base discrete weighted transform, FP64).
+ *
+ * The reference project (gpuLucas) is one executable whose routines are static
+ * functions over file-scope globals (gpuLucas.cu:179-257).  Each entry point below
+ * states which reference routine it replaces.  Conventions:
+ *   - every function returns an int status: GL_OK (0) or a negative GL_ERR_* code;
+ *     nothing here calls exit() (the reference exits on any CUDA error,
+ *     cuda_safecalls.h:37-98, and on an out-of-range ratio, gpuLucas.cu:327-331);
+ *   - a gl_plan owns all of its device memory and one CUDA stream; one host thread
+ *     uses a plan at a time; there is no global state;
+ *   - host buffers are owned by the caller.
+ */
+#ifndef GPULUCAS_H
+#define GPULUCAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GL_OK 0
+#define GL_ERR_ARG -1        /* bad argument (p, N, pointer, option) */
+#define GL_ERR_RATIO -2      /* p/N outside the carry-depth table (setSliceAndDice) */
+#define GL_ERR_SIZE -3       /* N not even, not 2^a 3^b 5^c 7^d, or no FFT layout */
+#define GL_ERR_CUDA -4       /* a CUDA runtime call failed */
+#define GL_ERR_NOMEM -5      /* device or host allocation failed / over budget */
+#define GL_ERR_ROUNDOFF -6   /* max round-off |x - rint(x)| reached the error limit */
+#define GL_ERR_OVERFLOW -7   /* a product left the range the carry slices cover */
+#define GL_ERR_NODEVICE -8   /* no CUDA device */
+#define GL_ERR_IO -9         /* checkpoint file could not be read or written */
+#define GL_ERR_CHECKPOINT -10 /* checkpoint does not match this test */
+#define GL_ERR_STATE -11     /* call not valid in the plan's current state */
+
+/* execution forms */
+#define GL_MODE_FUSED 0      /* 3 fused kernels per iteration (the product form) */
+#define GL_MODE_PLAIN 1      /* one kernel per reference step (comparison form) */
+
+typedef struct gl_plan gl_plan;
+
+typedef struct {
+    int mode;              /* GL_MODE_FUSED or GL_MODE_PLAIN */
+    int device;            /* CUDA device ordinal */
+    double error_limit;    /* abort when max round-off >= this (default 0.4) */
+    int check_every;       /* read the round-off status every K iterations (default 1000) */
+    int use_graphs;        /* capture iteration batches in CUDA graphs (default 1) */
+    int fft_h;             /* 0 = automatic; else force the column length H of M = W*H */
+    int cols_per_cta;      /* 0 = automatic; else columns per CTA in the column passes */
+    int reserved[8];
+} gl_plan_opts;
+
+typedef struct {
+    int p, N;
+    int lo_bits, hi_bits;  /* floor(p/N), floor(p/N)+1 (initConstantSymbols, gpuLucas.cu:222-237) */
+    int carry_depth;       /* n of llintToIrrBal<n> (setSliceAndDice, gpuLucas.cu:323-343) */
+    int mode;
+    int fft_w, fft_h;      /* N/2 = fft_w * fft_h complex points */
+    int cols_per_cta;
+    int radix_w[8], radix_h[8];
+    int threads_col, threads_row;  /* CTA sizes of the column and row passes */
+    int smem_col, smem_row;        /* dynamic shared memory bytes of those passes */
+    size_t device_bytes;   /* device memory held by the plan */
+} gl_plan_info;
+
+typedef struct {
+    int64_t iterations;    /* iterations done by this call */
+    int64_t total_iterations; /* iterations since S0 = 4 */
+    double max_roundoff;   /* max |x - rint(x)| seen by this call (checked iterations) */
+    double ms;             /* device time of the call, CUDA events */
+    int status;            /* GL_OK, GL_ERR_ROUNDOFF or GL_ERR_OVERFLOW */
+} gl_iter_report;
+
+typedef struct {
+    int p, N;
+    int64_t iterations;    /* LL iterations done (p - 2 for a full test) */
+    int is_prime;          /* residue == 0 mod 2^p - 1 after p - 2 iterations */
+    int is_zero;           /* exact zero test of the current residue */
+    uint64_t res64;        /* low 64 bits of S_k mod 2^p - 1 */
+    double max_roundoff;   /* over the run */
+    double ms;             /* device time */
+} gl_result;
+
+/* --- options and plans ------------------------------------------------ */
+int gl_default_opts(gl_plan_opts* opts);
+
+/* Replaces initConstantSymbols + setSliceAndDice + mallocArrays + computeBitsPerWord(Vectors)
+ * + computeWeightVectors + cufftPlan1d (gpuLucas.cu:222-237, 323-343, 948-1029, 673-714).
+ * N == 0 picks N with the autotuner (findSignalSize, gpuLucas.cu:1064-1187). */
+int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** plan);
+/* Replaces freeArrays (gpuLucas.cu:1031-1057). */
+int gl_plan_destroy(gl_plan* plan);
+int gl_plan_get_info(const gl_plan* plan, gl_plan_info* info);
+/* The layout gl_plan_create would choose for (p, N, opts), without touching a GPU. */
+int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info);
+
+/* Replaces loadValue4ToFFTarray (gpuLucas.cu:718-726): state := S0 = 4. */
+int gl_reset(gl_plan* plan);
+
+/* Runs `iters` LL iterations: the loop body mersenneIter<check,0> (gpuLucas.cu:845-942)
+ * with the round-off check of mersenneTest (gpuLucas.cu:1399-1410), aborting with
+ * GL_ERR_ROUNDOFF at the plan's error limit. */
+int gl_iterate(gl_plan* plan, int64_t iters, gl_iter_report* report);
+
+/* Asynchronous forms for callers that time or overlap work themselves: enqueue
+ * iterations on the plan's stream without waiting; read (and wait for) the status. */
+int gl_plan_stream(gl_plan* plan, void** cuda_stream);
+int gl_enqueue(gl_plan* plan, int64_t iters);
+int gl_sync_status(gl_plan* plan, gl_iter_report* report);
+/* kernel launches one iteration issues (3 for the fused form) */
+int gl_launches_per_iteration(const gl_plan* plan);
+
+/* The state after the last iteration. */
+int gl_get_products(gl_plan* plan, int64_t* ll_out);                     /* llint_signal, N int64 */
+int gl_get_carry_state(gl_plan* plan, int32_t* digit_out, int8_t* hi_out); /* i_signal, i_hiBitArr */
+/* Set the loop-carried products (llint_signal) and the iteration count; the next
+ * iteration, or gl_get_carry_state, dices them with llintToIrrBal<n>
+ * (IrrBaseBalanced.cu:52-110). */
+int gl_set_products(gl_plan* plan, const int64_t* ll, int64_t iterations);
+/* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */
+int gl_set_carry_state(gl_plan* plan, const int32_t* digit, const int8_t* hi, int64_t iterations);
+
+/* addPseudoBalanced + rebalanceIrrIntSEQGPU + print_residue + zero test
+ * (IrrBaseBalanced.cu:117-169, gpuLucas.cu:1288-1352, 1496-1512): rebalanced digits
+ * (may be NULL), Res64 and the exact zero test of the current state. */
+int gl_get_residue(gl_plan* plan, int32_t* digits_out, uint64_t* res64, int* is_zero);
+
+/* --- reference entry points (README: errorTest / mersenneTest) ---------- */
+
+/* errorTrial (gpuLucas.cu:1192-1282) as README's errorTest(p, N): runs
+ * clamp(p/10000, 100, 2500) iterations (gpuLucas.cu:529-541) and returns the average
+ * ms per iteration, or -1 when the round-off reached the limit (gpuLucas.cu:903-907). */
+float errorTest(int testPrime, int signalSize);
+/* mersenneTest (gpuLucas.cu:1358-1551) as README's mersenneTest(p, N): full p-2 iteration
+ * test.  Returns 1 if 2^p - 1 is prime, 0 if composite, a negative GL_ERR_* on error. */
+int mersenneTest(int testPrime, int signalSize);
+/* setSliceAndDice (gpuLucas.cu:323-343): carry depth n for p/N, extended to ratio 21;
+ * GL_ERR_RATIO for ratio >= 22. */
+int setSliceAndDice(int testPrime, int signalSize);
+
+/* Plan-based forms with full results. */
+int gl_error_test(int p, int N, const gl_plan_opts* opts, int iters, gl_iter_report* report);
+int gl_mersenne_test(gl_plan* plan, int64_t iters, gl_result* result);
+
+/* --- utilities ----------------------------------------------------------- */
+const char* gl_error_string(int status);
+int gl_version(void);        /* major*10000 + minor*100 + patch */
+/* FP64 throughput probe (DFMA), for the roofline denominator: TFLOP/s counting an FMA
+ * as 2 flops, measured on `device` for about `ms` milliseconds. */
+int gl_probe_fp64_peak(int device, double ms, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPULUCAS_H */

@@ -1,0 +1,80 @@
+"""The C-ABI library without a GPU: it loads, exports what include/gpulucas.h declares,
+validates arguments with status codes (never exit(), unlike cuda_safecalls.h:37-98),
+and picks sane FFT layouts (gl_plan_describe)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gpulucas.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+([A-Za-z_][A-Za-z0-9_]*)\s*\(", src, re.M)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported(gl):
+    names = header_functions()
+    assert len(names) >= 20
+    lib = ctypes.CDLL(gl.LIB_PATH)
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(gl.ABI_SYMBOLS) == names
+    out = subprocess.run(["nm", "-D", "--defined-only", gl.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert set(names) <= exported
+
+
+def test_library_is_built_for_sm_103a(gl):
+    from gpulucas_gb300 import _build
+    assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH)
+
+
+def test_status_strings(gl):
+    for code in range(0, -12, -1):
+        assert gl.error_string(code)
+
+
+@pytest.mark.parametrize("p,N,code", [(44497, 2047, -1), (44497, 2, -1), (1000, 2048, -1),
+                                      (50000, 2048, -2), (60013, 2 * 11 * 256, -3)])
+def test_describe_rejects(gl, p, N, code):
+    with pytest.raises(gl.GLError) as ei:
+        gl.describe(p, N)
+    assert ei.value.status == code
+
+
+@pytest.mark.parametrize("p,N", [(44497, 2048), (2976221, 163840), (43112609, 2359296), (100003, 5184),
+                                 (1000003, 54432), (2999999, 154350), (12379, 640), (300007, 15360)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_describe_layouts(gl, p, N, mode):
+    info = gl.describe(p, N, mode=mode)
+    M = N // 2
+    assert info.lo_bits == p // N and info.hi_bits == p // N + 1
+    assert info.carry_depth == gl.setSliceAndDice(p, N)
+    if mode == 0:
+        assert info.fft_w * info.fft_h == M
+        assert info.fft_w % info.cols_per_cta == 0
+        rw = [r for r in info.radix_w if r]
+        rh = [r for r in info.radix_h if r]
+        prod = lambda xs: eval("*".join(map(str, xs))) if xs else 1  # noqa: E731
+        assert prod(rw) == info.fft_w and prod(rh) == info.fft_h
+        assert set(rw + rh) <= {2, 3, 4, 5, 7, 8, 16}
+        assert info.smem_col == 2 * info.cols_per_cta * info.fft_h * 16 <= 200 * 1024
+        assert info.smem_row == 4 * info.fft_w * 16 <= 200 * 1024
+        assert 64 <= info.threads_col <= 512 and info.threads_col % 32 == 0
+        assert 64 <= info.threads_row <= 512 and info.threads_row % 32 == 0
+
+
+def test_plan_without_gpu_reports_status(gl):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(gl.GLError) as ei:
+        gl.Plan(44497, 2048)
+    assert ei.value.status == gl.GL_ERR_NODEVICE

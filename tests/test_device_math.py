@@ -1,0 +1,92 @@
+"""The kernels' arithmetic helpers (gl_device.cuh), compiled for the host, against numpy.
+
+Covers the small DFTs of every radix the line FFTs use, the integer-domain
+round-half-even that replaces __double2ll_rn (gpuLucas.cu:796) with its round-off
+distance, and the bit-built int -> double conversion of the weighted load
+(gpuLucas.cu:757).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from gpulucas_gb300 import _build
+
+
+@pytest.fixture(scope="module")
+def hc():
+    L = ctypes.CDLL(_build.HOSTCHECK)
+    L.hc_dft.argtypes = [ctypes.c_int, ctypes.c_int, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+    L.hc_dft.restype = ctypes.c_int
+    L.hc_round.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_int)]
+    L.hc_round.restype = ctypes.c_longlong
+    L.hc_dbl_from_int.argtypes = [ctypes.c_int]
+    L.hc_dbl_from_int.restype = ctypes.c_double
+    L.hc_dice_sum.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint,
+                              np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS"), ctypes.c_int, ctypes.c_int]
+    L.hc_dice_sum.restype = ctypes.c_longlong
+    L.hc_balanced_split.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_int)]
+    return L
+
+
+@pytest.mark.parametrize("R", [2, 3, 4, 5, 7, 8, 16])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_small_dft(hc, R, sign):
+    rng = np.random.default_rng(R * 10 + sign)
+    for _ in range(20):
+        x = rng.standard_normal(R) + 1j * rng.standard_normal(R)
+        buf = np.empty(2 * R)
+        buf[0::2], buf[1::2] = x.real, x.imag
+        assert hc.hc_dft(R, sign, buf) == 0
+        y = buf[0::2] + 1j * buf[1::2]
+        ref = np.fft.fft(x) if sign < 0 else np.fft.ifft(x) * R
+        assert np.abs(y - ref).max() <= 1e-14 * max(1.0, np.abs(ref).max())
+
+
+def _round(hc, x):
+    e = ctypes.c_ulonglong()
+    big = ctypes.c_int()
+    r = hc.hc_round(x, ctypes.byref(e), ctypes.byref(big))
+    return r, e.value / 2.0**64, big.value
+
+
+def test_round_half_even_matches_rint(hc):
+    rng = np.random.default_rng(7)
+    vals = list(rng.standard_normal(2000) * 1e6) + list(rng.standard_normal(2000) * 2.0**45)
+    vals += [0.0, -0.0, 0.5, 1.5, 2.5, -0.5, -1.5, -2.5, 3.4999999, 2.0**50 + 0.5, -(2.0**50) - 0.5,
+             1e-300, -1e-300, 0.49999999999999994, 2.0**-20, 7.0, -7.0]
+    for x in vals:
+        r, e, big = _round(hc, x)
+        assert big == 0
+        assert r == int(np.rint(x)), x
+        assert abs(e - abs(x - np.rint(x))) <= 2.0**-52, (x, e)
+
+
+def test_round_flags_unrepresentable(hc):
+    for x in [2.0**51, -(2.0**51), 2.0**60, 1e300]:
+        assert _round(hc, x)[2] == 1
+
+
+def test_int_to_double_exact(hc):
+    for v in list(range(-70000, 70000, 7)) + [2**30, -(2**30), 2**31 - 1, -(2**31) + 1, 1, -1, 0]:
+        assert hc.hc_dbl_from_int(v) == float(v)
+
+
+def test_dice_matches_oracle(hc, orc):
+    """llintToIrrBal<n> of the kernels vs the oracle's restatement on random products."""
+    rng = np.random.default_rng(3)
+    for p, N in [(44497, 2048), (100003, 5184), (12379, 640), (2976221, 163840)]:
+        n = orc.slice_depth(p, N)
+        LO = p // N
+        bits, flags = orc.bits(p, N)
+        ll = rng.integers(-(2**45), 2**45, N, dtype=np.int64)
+        ll[:5] = [0, -1, 1, 2**44, -(2**44)]
+        d_ref, h_ref = orc.dice(p, N, ll)
+        for j in list(range(8)) + list(rng.integers(0, N, 200)) + [N - 1]:
+            s = hc.hc_dice_sum(LO, n, int(flags[j]), ll, N, int(j))
+            d = ctypes.c_int()
+            h = ctypes.c_int()
+            hc.hc_balanced_split(s, LO + int(flags[j] & 1), ctypes.byref(d), ctypes.byref(h))
+            assert (d.value, h.value) == (int(d_ref[j]), int(h_ref[j])), (p, N, j)

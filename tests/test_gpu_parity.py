@@ -1,0 +1,110 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle, bit-exact.
+
+The loop-carried products (llint_signal) and the carry-save state (i_signal +
+i_hiBitArr) after k iterations must equal the oracle's restatement of the reference
+(gpuLucas.cu:845-942 mersenneIter, IrrBaseBalanced.cu:52-110 llintToIrrBal<n>) exactly:
+they are integers, so any difference is a bug, not round-off.  Residues are checked
+against the exact NTT oracle and the committed golden Res64 values.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+SMALL = [(44497, 2048), (100003, 5184), (12379, 640), (1000003, 54432), (86243, 4096)]
+
+
+def golden_res64():
+    with open(os.path.join(HERE, "golden", "res64.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("p,N", SMALL)
+@pytest.mark.parametrize("mode", [0, 1], ids=["fused", "plain"])
+def test_products_and_carry_state_match_oracle(gl, orc, p, N, mode):
+    with gl.Plan(p, N, mode=mode) as pl:
+        o = orc.IBDWT(p, N)
+        done = 0
+        for step in (1, 1, 2, 6, 30):
+            pl.iterate(step)
+            o.iterate(step)
+            done += step
+            ll = pl.products()
+            ref = o.ll()
+            bad = np.nonzero(ll != ref)[0]
+            assert bad.size == 0, f"iteration {done}: {bad.size} products differ, first {bad[:8]}"
+        d, h = pl.carry_state()
+        d2, h2 = o.state()
+        assert (d == d2).all() and (h == h2).all()
+        digits, r, z = pl.residue()
+        _, r2, _, z2 = o.residue()
+        assert r == r2 and z == z2
+        assert r == orc.Exact(p).iterate(done).res64()
+
+
+@pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432)])
+def test_dice_through_abi(gl, orc, p, N):
+    """llintToBalInt<n> semantics on arbitrary products via gl_set_products."""
+    rng = np.random.default_rng(p)
+    ll = rng.integers(-(2**44), 2**44, N, dtype=np.int64)
+    with gl.Plan(p, N) as pl:
+        pl.set_products(ll, 0)
+        d, h = pl.carry_state()
+    d2, h2 = orc.dice(p, N, ll)
+    assert (d == d2).all() and (h == h2).all()
+
+
+def test_fused_equals_plain_long_run(gl):
+    p, N = 1000003, 54432
+    with gl.Plan(p, N, mode=0) as a, gl.Plan(p, N, mode=1) as b:
+        a.iterate(700)
+        b.iterate(700)
+        assert (a.products() == b.products()).all()
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["fused", "plain"])
+def test_golden_res64(gl, mode):
+    for e in golden_res64():
+        p, N, k = e["p"], e["N"], e["k"]
+        if mode == 1 and k > 20000:
+            continue  # the plain form runs the long ones too slowly to be worth it here
+        with gl.Plan(p, N, mode=mode) as pl:
+            rep = pl.iterate(k)
+            _, r, z = pl.residue()
+        assert f"{r:016x}" == e["res64"], (p, N, k)
+        assert z == e["is_zero"]
+        assert rep.max_roundoff < 0.4
+
+
+def test_carry_state_resume(gl, orc):
+    """Stop, export the carry-save state, resume in a fresh plan: same products."""
+    p, N = 100003, 5184
+    with gl.Plan(p, N) as a:
+        a.iterate(300)
+        d, h = a.carry_state()
+        a.iterate(200)
+        ref = a.products()
+    with gl.Plan(p, N) as b:
+        b.set_carry_state(d, h, 300)
+        b.iterate(200)
+        assert (b.products() == ref).all()
+
+
+def test_mersenne_test_entry_points(gl):
+    assert gl.mersenneTest(44497, 2048) == 1
+    assert gl.mersenneTest(44501, 2048) == 0   # 44501 is prime, M44501 composite
+    ms = gl.errorTest(86243, 4096)
+    assert ms > 0
+
+
+def test_roundoff_abort_is_reported(gl):
+    """A too-small FFT length must stop with GL_ERR_ROUNDOFF, not trap or hang."""
+    with gl.Plan(44497, 2048, error_limit=0.05, check_every=50) as pl:
+        rep = pl.iterate(2000, check=False)
+        assert rep.status == gl.GL_ERR_ROUNDOFF
+        assert rep.iterations < 2000
