@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""bench.py -- Lucas-Lehmer iterations/s on GB300 (FP64 IBDWT, fused sm_103a kernels).
+
+Default workload: one LL iteration of the large single test p = 43112609 at
+N = 2359296 = 2^18 * 3^2 (18.27 bits/word), the length the reference quotes its own
+iteration rate at (gpuLucas.cu:92-97).  A step is one iteration; the L2 cache is
+flushed (512 MiB write) before every timed step, because the test's whole working set
+(about 110 MB) would otherwise stay L2-resident.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference's path (the oracle's IBDWT, all host threads) on the same workload.
+Under torchrun each rank runs an independent replica of the test (a single LL test
+does not shard: its FFT is global), value = iterations of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LL iter/s by FFT length vs plain same-GPU form"
+P3, N3 = 43112609, 2359296
+BY_LENGTH = [("c1", 44497, 2048), ("c2", 2976221, 163840), ("c3", P3, N3)]
+REF_PUBLISHED_ITER_S = 204.72  # gpuLucas.cu:92-96, p=42643801 at N=2359296 (GTX 480 / C2050)
+L2_FLUSH_BYTES = 512 << 20
+
+
+def flop_alg(N: int) -> float:
+    """5 N log2 N + 4 N: real forward + inverse FFT, square, weight, unweight."""
+    return 5.0 * N * math.log2(N) + 4.0 * N
+
+
+def kernel_flops(N: int, W: int, H: int) -> dict:
+    """flop_alg split over the three fused kernels (sums to flop_alg(N))."""
+    M = N // 2
+    return {
+        "k_col_fwd": 5.0 * M * math.log2(H) + N,
+        "k_row_sq": 10.0 * M * math.log2(W) + 10.0 * M + 2.0 * N,
+        "k_col_inv": 5.0 * M * math.log2(H) + N,
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms in the background."""
+
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={','.join(self.FIELDS)}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic_c3.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(kernel + " ") and "dram_bytes_per_launch=" in line:
+            try:
+                return float(line.split("dram_bytes_per_launch=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def cpu_baseline(p: int, N: int, budget_s: float = 12.0) -> dict:
+    """The oracle's IBDWT (the reference's algorithm on the CPU) on all host threads,
+    on a bounded sample of iterations of the same test."""
+    import oracle
+    threads = os.cpu_count() or 1
+    o = oracle.IBDWT(p, N, threads)
+    t0 = time.perf_counter()
+    o.iterate(1)
+    one = time.perf_counter() - t0
+    k = max(2, min(2000, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    o.iterate(k)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": k / dt, "unit": "iter/s", "cores": threads, "kind": "port",
+            "sample": f"{k} iterations of p={p} N={N} from S0=4 (after 1 warm-up), {dt:.1f} s"}
+
+
+def run_reference(args, world: int, rank: int):
+    if rank != 0:
+        return
+    import oracle
+    threads = os.cpu_count() or 1
+    o = oracle.IBDWT(P3, N3, threads)
+    for _ in range(max(1, args.warmup)):
+        o.iterate(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.iterate(1)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: the LL sequence from S0=4 (no dataset)",
+        "config": {"workload": f"LL iteration of p={P3} at N={N3} (2^18*3^2), CPU IBDWT restatement of "
+                               "the reference path (oracle/ibdwt_oracle.c), all host threads",
+                   "p": P3, "N": N3},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timed iterations after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def rate(gl, p, N, mode, seconds=0.4, device=0):
+    """Continuous (L2-warm) iterations/s of one form, for the by-length table."""
+    with gl.Plan(p, N, mode=mode, device=device, check_every=1 << 30) as pl:
+        pl.iterate(8)
+        k = 8
+        while True:
+            rep = pl.iterate(k)
+            if rep.ms * 1e-3 >= seconds or k >= 1 << 20:
+                return k / (rep.ms * 1e-3), rep.max_roundoff
+            k *= 2
+
+
+def run_ours(args, world: int, rank: int, local: int):
+    import numpy as np
+    import torch
+
+    import gpulucas_gb300 as gl
+
+    dev = local
+    torch.cuda.set_device(dev)
+    peak = gl.probe_fp64_peak(dev, 400.0)
+    plan = gl.Plan(P3, N3, device=dev, check_every=1 << 30)
+    info = plan.info
+    stream = torch.cuda.ExternalStream(plan.stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            flush.fill_(i & 0xFF)
+            plan.enqueue(1)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(dev)
+    sampler.start()
+    time.sleep(0.25)
+    barrier(world)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            plan.enqueue(1)
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    status = plan.sync_status(check=False)
+    total_ms_max = dist_max(total_ms, world)
+    value = world * args.steps / (total_ms_max * 1e-3)
+
+    # per-kernel device time and the roofline of the dominant kernel
+    prof = plan.profile_kernels(30)
+    kf = kernel_flops(N3, info.fft_w, info.fft_h)
+    dom = max(prof, key=prof.get)
+    achieved = kf[dom] / (prof[dom] * 1e-3) / 1e12
+    iter_ms = sum(prof.values())
+
+    # end to end through the C ABI with pinned host buffers: H2D carry state, one
+    # iteration, D2H carry state, every step
+    digit = torch.empty(N3, dtype=torch.int32).pin_memory()
+    hi = torch.empty(N3, dtype=torch.int8).pin_memory()
+    L = gl.lib
+    h = plan._h
+    rc = L.gl_get_carry_state(h, ctypes.c_void_p(digit.data_ptr()), ctypes.c_void_p(hi.data_ptr()))
+    assert rc == 0, rc
+    e2e_steps = max(10, min(200, args.steps // 4))
+    rep = gl.IterReport()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    base_iters = 0
+    for i in range(e2e_steps):
+        rc = L.gl_set_carry_state(h, ctypes.c_void_p(digit.data_ptr()), ctypes.c_void_p(hi.data_ptr()),
+                                  base_iters + i)
+        rc = rc or L.gl_iterate(h, 1, ctypes.byref(rep))
+        rc = rc or L.gl_get_carry_state(h, ctypes.c_void_p(digit.data_ptr()), ctypes.c_void_p(hi.data_ptr()))
+        assert rc == 0, rc
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist_max(e2e_s, world)
+    e2e = {"value": world * e2e_steps / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": N3 * 5,
+           "d2h_bytes_per_step": N3 * 5, "steps": e2e_steps,
+           "path": "gl_set_carry_state (H2D) + gl_iterate(1) + gl_get_carry_state (D2H), pinned buffers"}
+    plan.close()
+
+    line = {
+        "impl": "gpulucas_gb300", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / REF_PUBLISHED_ITER_S / world, "dtype": "f64",
+        "data": "synthetic: the LL sequence from S0=4 (no dataset)",
+        "config": {"workload": f"fused single LL test, one iteration of p={P3} at N={N3} (2^18*3^2)",
+                   "p": P3, "N": N3, "fft": f"{info.fft_h} x {info.fft_w}", "parallelism": "replicas",
+                   "l2": "flushed before every timed step (512 MiB write); working set ~110 MB < L2",
+                   "vs_baseline_note": "reference's published 204.72 iter/s at N=2359296 (GTX 480/C2050)"},
+        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": read_traffic(dom),
+                     "peak_source": "measured live: DFMA probe (gl_probe_fp64_peak); MEASURED_PEAKS.json has "
+                                    "no FP64 figure",
+                     "algorithmic_flops_per_launch": kf[dom], "kernel_ms": prof,
+                     "iteration_flop_alg": flop_alg(N3),
+                     "iteration_tflops": flop_alg(N3) / (iter_ms * 1e-3) / 1e12,
+                     "hbm_gbs_alg": 16.0 * N3 / (iter_ms * 1e-3) / 1e9},
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": args.steps * plan_launches(gl),
+        "max_roundoff": status.max_roundoff,
+    }
+    if rank == 0 and world == 1:
+        by = {}
+        for name, p, N in BY_LENGTH:
+            f, ef = rate(gl, p, N, gl.MODE_FUSED, device=dev)
+            pl_, ep = rate(gl, p, N, gl.MODE_PLAIN, device=dev)
+            by[name] = {"p": p, "N": N, "fused_iter_s": f, "plain_iter_s": pl_, "fused_over_plain": f / pl_,
+                        "fused_max_roundoff": ef, "plain_max_roundoff": ep, "l2": "warm (continuous run)"}
+        line["by_fft_length"] = by
+        line["cpu_baseline"] = cpu_baseline(P3, N3)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def plan_launches(gl) -> int:
+    return 3  # fused form: k_col_fwd, k_row_sq, k_col_inv per iteration
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        args.steps = min(args.steps, 200)
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

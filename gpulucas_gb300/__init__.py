@@ -83,6 +83,8 @@ def _load():
         "gl_enqueue": (ctypes.c_int, [P, ctypes.c_int64]),
         "gl_sync_status": (ctypes.c_int, [P, ctypes.POINTER(IterReport)]),
         "gl_launches_per_iteration": (ctypes.c_int, [P]),
+        "gl_profile_kernels": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_int)]),
         "gl_get_products": (ctypes.c_int, [P, vp]),
         "gl_get_carry_state": (ctypes.c_int, [P, vp, vp]),
         "gl_set_products": (ctypes.c_int, [P, vp, ctypes.c_int64]),
@@ -111,7 +113,8 @@ lib = _load()
 ABI_SYMBOLS = tuple(sorted([
     "gl_default_opts", "gl_plan_create", "gl_plan_destroy", "gl_plan_get_info", "gl_plan_describe",
     "gl_reset", "gl_iterate",
-    "gl_plan_stream", "gl_enqueue", "gl_sync_status", "gl_launches_per_iteration", "gl_get_products",
+    "gl_plan_stream", "gl_enqueue", "gl_sync_status", "gl_launches_per_iteration", "gl_profile_kernels",
+    "gl_get_products",
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
     "gl_probe_fp64_peak",
@@ -206,6 +209,14 @@ class Plan:
     @property
     def launches_per_iteration(self) -> int:
         return _check(lib.gl_launches_per_iteration(self._h), "launches")
+
+    def profile_kernels(self, iters: int = 10) -> dict:
+        """Average ms per launch of each fused kernel (events between launches)."""
+        ms = (ctypes.c_double * 3)()
+        names = (ctypes.c_char_p * 3)()
+        nk = ctypes.c_int()
+        _check(lib.gl_profile_kernels(self._h, int(iters), ms, names, ctypes.byref(nk)), "profile_kernels")
+        return {names[i].decode(): ms[i] for i in range(nk.value)}
 
     def products(self) -> np.ndarray:
         out = np.empty(self.N, np.int64)

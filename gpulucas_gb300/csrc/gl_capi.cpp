@@ -68,22 +68,54 @@ bool fill_line_plan(int L, LinePlan* lp) {
 
 int round_up32(int x) { return (x + 31) / 32 * 32; }
 
-// Pick M = W * H: both must factor into radices <= 16 and {3,5,7}; prefer H near
-// sqrt(M) and a power of two; two double-buffered rows must fit one CTA (W <= 3072).
-int choose_fused_geom(int M, int force_h, int force_g, FusedGeom* g) {
+// FP64 instructions per element of one line DFT with the given radices: the DFT_R
+// kernels of gl_device.cuh plus one complex twiddle product per non-first-stage input.
+double line_ops(const LinePlan& lp) {
+  auto dft_ops = [](int r) {
+    switch (r) {
+      case 2: return 4.0;
+      case 3: return 12.0;
+      case 4: return 16.0;
+      case 5: return 36.0;
+      case 7: return 72.0;
+      case 8: return 60.0;
+      default: return 150.0;  // 16
+    }
+  };
+  double ops = 0.0;
+  for (int s = 0; s < lp.nst; ++s) {
+    const int r = lp.radix[s];
+    ops += dft_ops(r) / r + (s ? 4.0 * (r - 1) / r : 0.0);
+  }
+  return ops;
+}
+
+int padded_stride(int L) { return L + (L >> 4) + 1; }
+
+// Pick M = W * H for `sms` SMs.  Work units: W columns (column passes, one per CTA)
+// and H/2+1 row pairs (row pass).  With equal units per kernel the busiest SM runs
+// ceil(units / sms) of them, so the modelled time is the sum over the three kernels
+// of ceil(units/sms) * FP64 instructions per unit.  Shared memory per CTA must fit
+// twice (two CTAs per SM at least) and blocks stay <= kMaxThreads.
+int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
+  if (sms <= 0) sms = 152;
   int bestH = 0;
-  double best = 1e30;
-  const double target = std::log2((double)M) / 2.0;
+  double best = 1e300;
   for (int H = 2; H <= M / 2; ++H) {
     if (M % H) continue;
     if (force_h && H != force_h) continue;
     const int W = M / H;
-    if (W > 3072 || H > 3072) continue;
+    if (W < 2) continue;
     LinePlan a, b;
     if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
-    double cost = std::fabs(std::log2((double)H) - target);
-    if (H & (H - 1)) cost += 0.75;  // odd factors in the column length
-    if (H & 1) cost += 2.0;
+    const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = (size_t)4 * padded_stride(W) * 16;
+    if (smc > 110 * 1024 || smr > 110 * 1024) continue;
+    if ((H + 15) / 16 > kMaxThreads) continue;
+    const double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
+    const double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * line_ops(a) + 16.0);
+    double cost = 2.0 * col + row;
+    // prefer smaller shared-memory footprints (more resident CTAs) on ties
+    cost *= 1.0 + 0.02 * (double)(smc + smr) / (64.0 * 1024);
     if (cost < best) {
       best = cost;
       bestH = H;
@@ -92,27 +124,19 @@ int choose_fused_geom(int M, int force_h, int force_g, FusedGeom* g) {
   if (!bestH) return GL_ERR_SIZE;
   g->H = bestH;
   g->W = M / bestH;
+  g->G = 1;
   fill_line_plan(g->W, &g->pw);
   fill_line_plan(g->H, &g->ph);
-  // columns per CTA: two shared buffers of G*H complex, at most 96 KiB when possible
-  int G = 1;
-  if (force_g) {
-    if (g->W % force_g) return GL_ERR_ARG;
-    G = force_g;
-  } else {
-    for (int c = 1; c <= 64 && c <= g->W; ++c)
-      if (g->W % c == 0 && (size_t)c * g->H * 32 <= 96 * 1024) G = c;
-  }
-  g->G = G;
-  g->sm_col = (size_t)2 * G * g->H * 16;
-  g->sm_row = (size_t)2 * 2 * g->W * 16;
-  if (g->sm_col > 200 * 1024 || g->sm_row > 200 * 1024) return GL_ERR_SIZE;
-  auto threads = [](int points) {
+  g->ls_col = padded_stride(g->H);
+  g->ls_row = padded_stride(g->W);
+  g->sm_col = (size_t)2 * g->ls_col * 16;
+  g->sm_row = (size_t)4 * g->ls_row * 16;
+  auto threads = [](int points, int cap) {
     int t = round_up32((points + 15) / 16);
-    return t < 64 ? 64 : (t > kMaxThreads ? kMaxThreads : t);
+    return t < 64 ? 64 : (t > cap ? cap : t);
   };
-  g->t_col = threads(G * g->H);
-  g->t_row = threads(2 * g->W);
+  g->t_col = threads(g->H, kMaxThreads);
+  g->t_row = threads(2 * g->W, kRowThreads);
   return GL_OK;
 }
 
@@ -303,12 +327,15 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   const int M = N / 2;
   FusedGeom fg{};
   PlainGeom pg{};
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, o.fft_h, o.cols_per_cta, &fg) : choose_plain_geom(M, &pg);
-  if (rc != GL_OK) return rc;
+  if (o.cols_per_cta > 1) return GL_ERR_ARG;  // the column passes take one column per CTA
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GL_ERR_NODEVICE;
   if (o.device < 0 || o.device >= ndev) return GL_ERR_ARG;
   if (cudaSetDevice(o.device) != cudaSuccess) return GL_ERR_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess) return GL_ERR_CUDA;
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, o.fft_h, sms, &fg) : choose_plain_geom(M, &pg);
+  if (rc != GL_OK) return rc;
 
   gl_plan* pl = new (std::nothrow) gl_plan();
   if (!pl) return GL_ERR_NOMEM;
@@ -335,7 +362,7 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   std::vector<int32_t> bits;
   std::vector<uint8_t> flags;
   std::vector<double> A, Ainv;
-  std::vector<HostCplx> twM, twW, twH;
+  std::vector<HostCplx> twM;
   word_tables(p, N, bits, flags);
   weight_tables(p, N, 2.0 * N, A, Ainv);
   twiddle_table(M, twM);
@@ -343,9 +370,10 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   IterArgs& a = pl->args;
   a.N = N; a.M = M; a.LO = pl->LO; a.n = n;
   long long* ll;
-  unsigned char* fl;
+  unsigned char *fl, *span = nullptr;
   double *dA, *dAi;
-  DevCplx *Z, *Z2 = nullptr, *dtwM, *dtwW = nullptr, *dtwH = nullptr;
+  DevCplx *Z, *Z2 = nullptr, *dtwM = nullptr, *dtwW = nullptr, *dtwH = nullptr;
+  DevCplx *dK1 = nullptr, *dPair = nullptr, *dK2 = nullptr;
   int* digit;
   signed char* hi;
   Status* status;
@@ -354,27 +382,63 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   GL_TRY(dev_alloc(pl, &dA, N));
   GL_TRY(dev_alloc(pl, &dAi, N));
   GL_TRY(dev_alloc(pl, &Z, M));
-  GL_TRY(dev_alloc(pl, &dtwM, M));
   GL_TRY(dev_alloc(pl, &digit, N));
   GL_TRY(dev_alloc(pl, &hi, N));
   GL_TRY(dev_alloc(pl, &status, 1));
-  if (o.mode == GL_MODE_PLAIN) GL_TRY(dev_alloc(pl, &Z2, M));
-  if (o.mode == GL_MODE_FUSED) {
-    twiddle_table(fg.W, twW);
-    twiddle_table(fg.H, twH);
-    GL_TRY(dev_alloc(pl, &dtwW, fg.W));
-    GL_TRY(dev_alloc(pl, &dtwH, fg.H));
-    GL_TRYC(cudaMemcpy(dtwW, twW.data(), sizeof(DevCplx) * fg.W, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dtwH, twH.data(), sizeof(DevCplx) * fg.H, cudaMemcpyHostToDevice));
-    a.W = fg.W; a.H = fg.H; a.G = fg.G; a.pw = fg.pw; a.ph = fg.ph;
+  if (o.mode == GL_MODE_PLAIN) {
+    GL_TRY(dev_alloc(pl, &Z2, M));
+    GL_TRY(dev_alloc(pl, &dtwM, M));
+    GL_TRYC(cudaMemcpy(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(fl, flags.data(), N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  } else {
+    const int W = fg.W, H = fg.H;
+    // per-word tables in column-major order: word j = 2(m1 + W m2) + e -> 2(m1 H + m2) + e
+    std::vector<uint8_t> fl_c(N), span_c(N);
+    std::vector<double> A_c(N), Ai_c(N);
+    for (int j = 0; j < N; ++j) {
+      const int m = j >> 1, m1 = m % W, m2 = m / W;
+      const int c = 2 * (m1 * H + m2) + (j & 1);
+      fl_c[c] = flags[j];
+      A_c[c] = A[j];
+      Ai_c[c] = Ainv[j];
+      int tot = 0;
+      for (int i = 0; i <= n; ++i) tot += bits[(j + i) % N];
+      span_c[c] = (uint8_t)(tot > 255 ? 255 : tot);
+    }
+    std::vector<int> rw(fg.pw.radix, fg.pw.radix + fg.pw.nst), rh(fg.ph.radix, fg.ph.radix + fg.ph.nst);
+    std::vector<HostCplx> twW, twH, tK1((size_t)M), tPair((size_t)M), tK2((size_t)M);
+    stage_twiddles(W, rw, twW);
+    stage_twiddles(H, rh, twH);
+    for (int k2 = 0; k2 < H; ++k2)
+      for (int m1 = 0; m1 < W; ++m1) {
+        const HostCplx w = twM[(size_t)m1 * k2];   // m1 * k2 < M
+        tK1[(size_t)m1 * H + k2] = w;
+        tK2[(size_t)k2 * W + m1] = w;
+        tPair[(size_t)k2 * W + m1] = twM[(size_t)k2 + (size_t)H * m1];
+      }
+    GL_TRY(dev_alloc(pl, &span, N));
+    GL_TRY(dev_alloc(pl, &dtwW, twW.size()));
+    GL_TRY(dev_alloc(pl, &dtwH, twH.size()));
+    GL_TRY(dev_alloc(pl, &dK1, M));
+    GL_TRY(dev_alloc(pl, &dPair, M));
+    GL_TRY(dev_alloc(pl, &dK2, M));
+    GL_TRYC(cudaMemcpy(fl, fl_c.data(), N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(span, span_c.data(), N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dA, A_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dAi, Ai_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dtwW, twW.data(), sizeof(DevCplx) * twW.size(), cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dtwH, twH.data(), sizeof(DevCplx) * twH.size(), cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dK1, tK1.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dPair, tPair.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dK2, tK2.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    a.W = W; a.H = H; a.G = 1; a.pw = fg.pw; a.ph = fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
     GL_TRYC(set_fused_smem_limits(fg));
   }
-  GL_TRYC(cudaMemcpy(fl, flags.data(), N, cudaMemcpyHostToDevice));
-  GL_TRYC(cudaMemcpy(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-  GL_TRYC(cudaMemcpy(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-  GL_TRYC(cudaMemcpy(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-  a.ll = ll; a.flags = fl; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;
-  a.twM = dtwM; a.twW = dtwW; a.twH = dtwH; a.digit = digit; a.hi = hi; a.status = status;
+  a.ll = ll; a.flags = fl; a.span = span; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;
+  a.twM = dtwM; a.twW = dtwW; a.twH = dtwH; a.twK1 = dK1; a.twPair = dPair; a.twK2 = dK2;
+  a.digit = digit; a.hi = hi; a.status = status;
   *out = pl;
   int r = gl_reset(pl);
   if (r != GL_OK) {
@@ -398,15 +462,21 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
   if (n < 0) return GL_ERR_RATIO;
   gl_plan tmp;
   tmp.p = p; tmp.N = N; tmp.M = N / 2; tmp.LO = p / N; tmp.n = n; tmp.mode = o.mode;
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, o.cols_per_cta, &tmp.fg)
+  if (o.cols_per_cta > 1) return GL_ERR_ARG;
+  int sms = 0, ndev = 0;
+  if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && o.device >= 0 && o.device < ndev)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device);
+  if (sms <= 0) sms = 152;  // GB300
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg)
                                    : choose_plain_geom(tmp.M, &tmp.pg);
   if (rc != GL_OK) return rc;
   tmp.device = -1;
   int r = gl_plan_get_info(&tmp, info);
   if (o.mode == GL_MODE_FUSED) {
     const size_t M = tmp.M, N8 = (size_t)N * 8;
-    info->device_bytes = N8 /*ll*/ + N /*flags*/ + 2 * N8 /*A, Ainv*/ + 2 * M * 16 /*Z, twM*/ +
-                         (size_t)(tmp.fg.W + tmp.fg.H) * 16 + (size_t)N * 5 + 16;
+    info->device_bytes = N8 /*ll*/ + 2 * (size_t)N /*flags, span*/ + 2 * N8 /*A, Ainv*/ +
+                         4 * M * 16 /*Z, 3 twiddle tables*/ + (size_t)(tmp.fg.W + tmp.fg.H) * 16 +
+                         (size_t)N * 5 /*digit, hi*/ + 16;
   }
   return r;
 }
@@ -528,17 +598,66 @@ int gl_launches_per_iteration(const gl_plan* pl) {
   return 2 * pl->pg.nst + 4;
 }
 
+int gl_profile_kernels(gl_plan* pl, int iters, double* ms_out, const char** names, int* nk) {
+  if (!pl || !ms_out || iters < 1) return GL_ERR_ARG;
+  if (pl->mode != GL_MODE_FUSED) return GL_ERR_STATE;
+  GL_CUDA(cudaSetDevice(pl->device));
+  static const char* kNames[3] = {"k_col_fwd", "k_row_sq", "k_col_inv"};
+  if (pl->from_state) {  // consume a pending state load first
+    int rc = launch_iterations(pl, 1);
+    if (rc != GL_OK) return rc;
+    pl->iters_done += 1;
+  }
+  cudaEvent_t ev[4];
+  for (auto& e : ev) GL_CUDA(cudaEventCreate(&e));
+  double acc[3] = {0, 0, 0};
+  int rc = GL_OK;
+  for (int it = 0; it < iters && rc == GL_OK; ++it) {
+    for (int k = 0; k < 3; ++k) {
+      if (cudaEventRecord(ev[k], pl->stream) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
+      if (launch_fused_kernel(pl->args, pl->fg, pl->stream, k) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
+    }
+    if (rc != GL_OK) break;
+    if (cudaEventRecord(ev[3], pl->stream) != cudaSuccess || cudaEventSynchronize(ev[3]) != cudaSuccess) {
+      rc = GL_ERR_CUDA;
+      break;
+    }
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      acc[k] += ms;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc != GL_OK) return rc;
+  pl->iters_done += iters;
+  pl->carry_valid = false;
+  for (int k = 0; k < 3; ++k) {
+    ms_out[k] = acc[k] / iters;
+    if (names) names[k] = kNames[k];
+  }
+  if (nk) *nk = 3;
+  return GL_OK;
+}
+
 int gl_get_products(gl_plan* pl, int64_t* ll_out) {
   if (!pl || !ll_out) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));
-  GL_CUDA(cudaMemcpyAsync(ll_out, pl->args.ll, sizeof(int64_t) * pl->N, cudaMemcpyDeviceToHost, pl->stream));
+  const long long* src = pl->args.ll;
+  if (pl->mode == GL_MODE_FUSED) {  // un-permute into the (idle) work array
+    long long* tmp = reinterpret_cast<long long*>(pl->args.Z);
+    GL_CUDA(launch_permute_words(pl->args, pl->args.ll, tmp, false, pl->stream));
+    src = tmp;
+  }
+  GL_CUDA(cudaMemcpyAsync(ll_out, src, sizeof(int64_t) * pl->N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaStreamSynchronize(pl->stream));
   return GL_OK;
 }
 
 static int ensure_carry(gl_plan* pl) {
   if (!pl->carry_valid) {
-    GL_CUDA(launch_dice(pl->args, pl->stream));
+    if (pl->mode == GL_MODE_FUSED) GL_CUDA(launch_dice_perm(pl->args, pl->stream));
+    else GL_CUDA(launch_dice(pl->args, pl->stream));
     pl->carry_valid = true;
   }
   return GL_OK;
@@ -558,7 +677,13 @@ int gl_get_carry_state(gl_plan* pl, int32_t* digit_out, int8_t* hi_out) {
 int gl_set_products(gl_plan* pl, const int64_t* ll, int64_t iterations) {
   if (!pl || !ll || iterations < 0) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));
-  GL_CUDA(cudaMemcpyAsync(pl->args.ll, ll, sizeof(int64_t) * pl->N, cudaMemcpyHostToDevice, pl->stream));
+  if (pl->mode == GL_MODE_FUSED) {
+    long long* tmp = reinterpret_cast<long long*>(pl->args.Z);
+    GL_CUDA(cudaMemcpyAsync(tmp, ll, sizeof(int64_t) * pl->N, cudaMemcpyHostToDevice, pl->stream));
+    GL_CUDA(launch_permute_words(pl->args, tmp, pl->args.ll, true, pl->stream));
+  } else {
+    GL_CUDA(cudaMemcpyAsync(pl->args.ll, ll, sizeof(int64_t) * pl->N, cudaMemcpyHostToDevice, pl->stream));
+  }
   GL_CUDA(cudaStreamSynchronize(pl->stream));
   pl->iters_done = iterations;
   pl->from_state = false;

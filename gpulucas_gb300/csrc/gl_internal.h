@@ -9,7 +9,9 @@
 namespace gl {
 
 // the fused kernels are compiled for at most this many threads per CTA
-constexpr int kMaxThreads = 512;
+constexpr int kMaxThreads = 256;
+// the row pass (two lines, two buffers) is compiled for at most 128 threads, 3 CTAs/SM
+constexpr int kRowThreads = 128;
 
 struct DevCplx {
   double re, im;
@@ -32,9 +34,12 @@ constexpr unsigned kStatusBig = 1u;    // |product| >= 2^51: doubles cannot hold
 constexpr unsigned kStatusSlice = 2u;  // product bits beyond what n+1 slices place
 
 // Geometry of the fused form: the N/2 complex points are an H x W array
-// (row-major, element m = m1 + W*m2); column passes take G columns per CTA.
+// (element m = m1 + W*m2); each column pass CTA takes one column (G = 1), each row
+// pass CTA one row pair.  Per-word data of the fused form (products, weights, flags)
+// is stored column-major: word j = 2(m1 + W m2) + e lives at 2(m1 H + m2) + e.
 struct FusedGeom {
   int W, H, G;
+  int ls_col, ls_row;        // padded shared-memory line strides (complex)
   int t_col, t_row;          // threads per CTA
   size_t sm_col, sm_row;     // dynamic shared memory bytes
   LinePlan pw, ph;
@@ -49,15 +54,20 @@ struct PlainGeom {
 // Arguments of one iteration (passed by value to every kernel).
 struct IterArgs {
   int N, M, W, H, G, LO, n;
-  long long* ll;              // loop-carried products, N int64 (fused)
-  const unsigned char* flags; // bitsPerWord8, N
-  const double* A;            // N weights
-  const double* Ainv;         // N inverse weights with 1/(2N) folded in
+  int ls_col, ls_row;
+  long long* ll;              // loop-carried products, N int64 (fused: column-major)
+  const unsigned char* flags; // bitsPerWord8, N (fused: column-major)
+  const unsigned char* span;  // fused: bits product j may place into words j..j+n (column-major)
+  const double* A;            // N weights (fused: column-major)
+  const double* Ainv;         // N inverse weights with 1/(2N) folded in (fused: column-major)
   DevCplx* Z;                 // M complex work array [H][W]
   DevCplx* Z2;                // M complex (plain: ping-pong)
   const DevCplx* twM;         // exp(-2 pi i t/M), t < M
-  const DevCplx* twW;         // exp(-2 pi i t/W), t < W
-  const DevCplx* twH;         // exp(-2 pi i t/H), t < H
+  const DevCplx* twW;         // stage-ordered twiddles of the length-W line DFT
+  const DevCplx* twH;         // stage-ordered twiddles of the length-H line DFT
+  const DevCplx* twK1;        // w_M^(m1 k2) at m1*H + k2 (column pass output)
+  const DevCplx* twPair;      // w_M^(k2 + H k1) at k2*W + k1 (real-signal split)
+  const DevCplx* twK2;        // w_M^(m1 k2) at k2*W + m1 (row pass output)
   int* digit;                 // plain: i_signal, N
   signed char* hi;            // plain: i_hiBitArr, N
   Status* status;
@@ -68,10 +78,17 @@ struct IterArgs {
 // from_state: the first column pass loads the carry-save state (digit, hi) instead of
 // dicing the products, exactly as loadIntToDoubleIBDWT (gpuLucas.cu:730-766) does
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state);
+// one of the three fused kernels (0 = k_col_fwd, 1 = k_row_sq, 2 = k_col_inv)
+cudaError_t launch_fused_kernel(const IterArgs& a, const FusedGeom& g, cudaStream_t s, int which);
 cudaError_t launch_plain_iteration(const IterArgs& a, const PlainGeom& g, cudaStream_t s);
 cudaError_t launch_set_initial(const IterArgs& a, int mode, cudaStream_t s);
 // carry-save state (digit, hi) = dice(ll) for the fused form; plain keeps it already
 cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
+// fused form: dice the column-major products into natural-order (digit, hi)
+cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
+// fused form: natural <-> column-major copies of an int64 word array
+cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
+                                 cudaStream_t s);
 cudaError_t set_fused_smem_limits(const FusedGeom& g);
 cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s);
 

@@ -38,36 +38,42 @@ __device__ __forceinline__ void st(DevCplx* p, cplx v) {
 }
 
 // ---------------------------------------------------------------------------
-// Stockham DIT stage in shared memory, out of place (src -> dst, one barrier).
-// Butterfly j of a line reads src[j + q L/R], twiddles by w_L^((j mod Ns) q L/(Ns R)),
-// does DFT_R and writes dst[(j - j mod Ns) R + j mod Ns + q Ns].  Each thread keeps
-// one butterfly live at a time, so any block size works.
+// Shared-memory line FFTs.  Element i of a line sits at pad(i) = i + i/16: the
+// Stockham writes of a stage with span 1 go to stride-R addresses, which without
+// the pad would all fall into one bank group.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+
+// Stockham DIT stage, out of place (src -> dst, one barrier).  Butterfly j of a
+// line reads x[j + q L/R], twiddles by w_L^((j mod Ns) q L/(Ns R)), does DFT_R and
+// writes x[(j - j mod Ns) R + j mod Ns + q Ns].  Twiddles come from the stage-ordered
+// table: entry (Ns - 1) + (q - 1) Ns + k.
 template <int R, int S>
 __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cplx* __restrict__ dst, int nlines,
                                                int ls, int L, int Ns, const DevCplx* __restrict__ tw) {
   const int LR = L / R;
   const int nb = nlines * LR;
-  const int tws = L / (Ns * R);
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     const int l = b / LR;
     const int j = b - l * LR;
     const int k = j % Ns;
-    const cplx* s = src + l * ls + j;
+    const cplx* s = src + l * ls;
     cplx v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = s[q * LR];
+    for (int q = 0; q < R; ++q) v[q] = s[pad(j + q * LR)];
     if (Ns > 1) {
+      const DevCplx* t = tw + (Ns - 1) + k;
 #pragma unroll
       for (int q = 1; q < R; ++q) {
-        const cplx w = ld(tw + k * q * tws);
+        const cplx w = ld(t + (q - 1) * Ns);
         v[q] = (S < 0) ? cmul(v[q], w) : cmulc(v[q], w);
       }
     }
     dft<R, S>(v);
-    cplx* d = dst + l * ls + (j - k) * R + k;
+    cplx* d = dst + l * ls;
+    const int base = (j - k) * R + k;
 #pragma unroll
-    for (int q = 0; q < R; ++q) d[q * Ns] = v[q];
+    for (int q = 0; q < R; ++q) d[pad(base + q * Ns)] = v[q];
   }
   __syncthreads();
 }
@@ -113,119 +119,138 @@ __device__ __forceinline__ void pair_square(cplx u, cplx up, cplx w, cplx* vk, c
   *vkp = mk(fma(2.0, r.im, pr), fma(2.0, r.re, -pi));
 }
 
-// ---------------------------------------------------------------------------
-// Dicing helpers over the loop-carried products
-// ---------------------------------------------------------------------------
-struct WordSums {
-  int v0, v1;  // digit + carry of the word below, for words j0 and j0+1
-};
-
-// words j0 = 2m, j0+1: digit sums of j0-1, j0, j0+1 from ll[j0-1-n .. j0+1]
-__device__ __forceinline__ WordSums load_words(const IterArgs& a, int j0) {
-  const long long* __restrict__ ll = a.ll;
-  const unsigned char* __restrict__ fl = a.flags;
-  const int N = a.N;
-  auto at = [&](int j) -> long long { return __ldg(ll + (j < 0 ? j + N : j)); };
-  const int jm = j0 == 0 ? N - 1 : j0 - 1;
-  const uint32_t fm = __ldg(fl + jm), f0 = __ldg(fl + j0), f1 = __ldg(fl + j0 + 1);
-  const long long sm1 = dice_sum(a.LO, a.n, fm, [&](int i) { return at(jm - i); });
-  const long long s0 = dice_sum(a.LO, a.n, f0, [&](int i) { return at(j0 - i); });
-  const long long s1 = dice_sum(a.LO, a.n, f1, [&](int i) { return at(j0 + 1 - i); });
-  int dm, hm, d0, h0, d1, h1;
-  balanced_split(sm1, a.LO + (int)(fm & 1), &dm, &hm);
-  balanced_split(s0, a.LO + (int)(f0 & 1), &d0, &h0);
-  balanced_split(s1, a.LO + (int)(f1 & 1), &d1, &h1);
-  WordSums w;
-  w.v0 = d0 + hm;
-  w.v1 = d1 + h0;
-  return w;
-}
-
-__device__ __forceinline__ WordSums load_state(const IterArgs& a, int j0) {
-  const int jm = j0 == 0 ? a.N - 1 : j0 - 1;
-  WordSums w;
-  w.v0 = a.digit[j0] + (int)a.hi[jm];
-  w.v1 = a.digit[j0 + 1] + (int)a.hi[j0];
-  return w;
+// column-major position of natural word j (fused form layout)
+__device__ __forceinline__ int colmajor(const IterArgs& a, int j) {
+  const int m = j >> 1;
+  const int m2 = m / a.W;
+  const int m1 = m - m2 * a.W;
+  return 2 * (m1 * a.H + m2) + (j & 1);
 }
 
 // ---------------------------------------------------------------------------
-// Fused kernels
+// Fused kernels (one column / one row pair per CTA)
 // ---------------------------------------------------------------------------
-template <bool FROM_STATE>
-__global__ void __launch_bounds__(kMaxThreads) k_col_fwd(IterArgs a) {
+
+// Column pass, forward.  NC = carry depth n of llintToIrrBal<n>.  For words
+// j0 = 2m, j0+1 the digit sums of j0-1, j0, j0+1 need the products of words
+// j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.
+template <bool FROM_STATE, int NC>
+__global__ void __launch_bounds__(kMaxThreads, 2) k_col_fwd(IterArgs a) {
   extern __shared__ cplx smem[];
-  const int G = a.G, H = a.H, W = a.W;
-  const int c0 = blockIdx.x * G;
-  const int ls = H;
-  cplx* buf1 = smem + G * H;
-  for (int idx = threadIdx.x; idx < G * H; idx += blockDim.x) {
-    const int l = idx % G, m2 = idx / G;
-    const int j0 = 2 * (c0 + l + W * m2);
-    const WordSums w = FROM_STATE ? load_state(a, j0) : load_words(a, j0);
-    const double x0 = __ldg(a.A + j0) * dbl_from_int(w.v0);
-    const double x1 = __ldg(a.A + j0 + 1) * dbl_from_int(w.v1);
-    smem[l * ls + m2] = mk(x0, x1);
+  const int H = a.H, W = a.W, N = a.N;
+  const int ls = a.ls_col;
+  const int m1 = blockIdx.x;
+  cplx* buf1 = smem + ls;
+  for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
+    const int j0 = 2 * (m1 + W * m2);
+    const int s0 = 2 * (m1 * H + m2);
+    int v0, v1;
+    if (FROM_STATE) {
+      v0 = a.digit[j0] + (int)a.hi[j0 == 0 ? N - 1 : j0 - 1];
+      v1 = a.digit[j0 + 1] + (int)a.hi[j0];
+    } else {
+      long long P[NC + 3];
+      const longlong2 own = __ldg(reinterpret_cast<const longlong2*>(a.ll + s0));
+      P[0] = own.y;
+      P[1] = own.x;
+#pragma unroll
+      for (int k = 2; k < NC + 3; ++k) {
+        int j = j0 + 1 - k;
+        if (j < 0) j += N;
+        P[k] = __ldg(a.ll + colmajor(a, j));
+      }
+      const int jm = j0 == 0 ? N - 1 : j0 - 1;
+      const uint32_t f0 = __ldg(a.flags + s0), f1 = __ldg(a.flags + s0 + 1);
+      const uint32_t fm = __ldg(a.flags + colmajor(a, jm));
+      long long sm1 = 0, sw0 = 0, sw1 = 0;
+      {
+        const int LO = a.LO;
+        auto dice_at = [&](uint32_t f, int off) {
+          const long long mask = (1ll << (LO + (int)(f & 1))) - 1;
+          const long long v = P[off];
+          long long sum = v < 0 ? -((-v) & mask) : (v & mask);
+          int shift = 0;
+#pragma unroll
+          for (int i = 1; i <= NC; ++i) {
+            shift += LO + (int)((f >> i) & 1);
+            const long long w = P[off + i];
+            sum += shift >= 63 ? 0 : (w < 0 ? -(((-w) >> shift) & mask) : ((w >> shift) & mask));
+          }
+          return sum;
+        };
+        sw1 = dice_at(f1, 0);
+        sw0 = dice_at(f0, 1);
+        sm1 = dice_at(fm, 2);
+      }
+      int dm, hm, d0, h0, d1, h1;
+      balanced_split(sm1, a.LO + (int)(fm & 1), &dm, &hm);
+      balanced_split(sw0, a.LO + (int)(f0 & 1), &d0, &h0);
+      balanced_split(sw1, a.LO + (int)(f1 & 1), &d1, &h1);
+      v0 = d0 + hm;
+      v1 = d1 + h0;
+    }
+    const double2 A = __ldg(reinterpret_cast<const double2*>(a.A + s0));
+    smem[pad(m2)] = mk(A.x * dbl_from_int(v0), A.y * dbl_from_int(v1));
   }
   __syncthreads();
-  const cplx* res = line_fft<-1>(smem, buf1, G, ls, a.ph, a.twH);
-  for (int idx = threadIdx.x; idx < G * H; idx += blockDim.x) {
-    const int l = idx % G, k2 = idx / G;
-    const int m1 = c0 + l;
-    const cplx v = cmul(res[l * ls + k2], ld(a.twM + m1 * k2));
-    st(a.Z + k2 * W + m1, v);
-  }
+  const cplx* res = line_fft<-1>(smem, buf1, 1, ls, a.ph, a.twH);
+  const DevCplx* tw = a.twK1 + (size_t)m1 * H;
+  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x)
+    st(a.Z + (size_t)k2 * W + m1, cmul(res[pad(k2)], ld(tw + k2)));
 }
 
-__global__ void __launch_bounds__(kMaxThreads) k_row_sq(IterArgs a) {
+__global__ void __launch_bounds__(kRowThreads, 3) k_row_sq(IterArgs a) {
   extern __shared__ cplx smem[];
   const int W = a.W, H = a.H;
+  const int ls = a.ls_row;
   const int c = blockIdx.x;  // 0 .. H/2
   const int ra = c, rb = H - c;
   const bool self = (c == 0) || (2 * c == H);
   const int nl = self ? 1 : 2;
-  cplx* buf1 = smem + 2 * W;
+  cplx* buf1 = smem + 2 * ls;
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
-    const int l = idx / W, k1 = idx - l * W;
-    smem[idx] = ldc(a.Z + (l ? rb : ra) * W + k1);
+    const int l = idx >= W;
+    const int k1 = idx - l * W;
+    smem[l * ls + pad(k1)] = ldc(a.Z + (size_t)(l ? rb : ra) * W + k1);
   }
   __syncthreads();
-  cplx* sp = line_fft<-1>(smem, buf1, nl, W, a.pw, a.twW);
+  cplx* sp = line_fft<-1>(smem, buf1, nl, ls, a.pw, a.twW);
   cplx* other = sp == smem ? buf1 : smem;
+  const DevCplx* twp = a.twPair + (size_t)ra * W;
   if (!self) {
     for (int t = threadIdx.x; t < W; t += blockDim.x) {
       const int tp = W - 1 - t;
       cplx vk, vkp;
-      pair_square(sp[t], sp[W + tp], ld(a.twM + ra + H * t), &vk, &vkp);
-      sp[t] = vk;
-      sp[W + tp] = vkp;
+      pair_square(sp[pad(t)], sp[ls + pad(tp)], ld(twp + t), &vk, &vkp);
+      sp[pad(t)] = vk;
+      sp[ls + pad(tp)] = vkp;
     }
   } else if (c == 0) {
     // row 0: frequency H*t pairs with H*((W - t) mod W)
     for (int t = threadIdx.x; t <= W / 2; t += blockDim.x) {
       const int tp = (W - t) % W;
       cplx vk, vkp;
-      pair_square(sp[t], sp[tp], ld(a.twM + H * t), &vk, &vkp);
-      sp[t] = vk;
-      if (tp != t) sp[tp] = vkp;
+      pair_square(sp[pad(t)], sp[pad(tp)], ld(twp + t), &vk, &vkp);
+      sp[pad(t)] = vk;
+      if (tp != t) sp[pad(tp)] = vkp;
     }
   } else {
     // row H/2: frequency H/2 + H*t pairs with H/2 + H*(W-1-t)
     for (int t = threadIdx.x; t < (W + 1) / 2; t += blockDim.x) {
       const int tp = W - 1 - t;
       cplx vk, vkp;
-      pair_square(sp[t], sp[tp], ld(a.twM + ra + H * t), &vk, &vkp);
-      sp[t] = vk;
-      if (tp != t) sp[tp] = vkp;
+      pair_square(sp[pad(t)], sp[pad(tp)], ld(twp + t), &vk, &vkp);
+      sp[pad(t)] = vk;
+      if (tp != t) sp[pad(tp)] = vkp;
     }
   }
   __syncthreads();
-  const cplx* res = line_fft<+1>(sp, other, nl, W, a.pw, a.twW);
+  const cplx* res = line_fft<+1>(sp, other, nl, ls, a.pw, a.twW);
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
-    const int l = idx / W, m1 = idx - l * W;
+    const int l = idx >= W;
+    const int m1 = idx - l * W;
     const int row = l ? rb : ra;
-    const cplx v = cmulc(res[idx], ld(a.twM + m1 * row));
-    st(a.Z + row * W + m1, v);
+    st(a.Z + (size_t)row * W + m1, cmulc(res[l * ls + pad(m1)], ld(a.twK2 + (size_t)row * W + m1)));
   }
 }
 
@@ -238,7 +263,7 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
-// bits that product j can place into words j..j+n
+// bits that product j can place into words j..j+n, natural order (plain form)
 __device__ __forceinline__ int slice_span(const IterArgs& a, int j) {
   int jn = j + a.n;
   if (jn >= a.N) jn -= a.N;
@@ -255,60 +280,119 @@ __device__ __forceinline__ void finish_status(const IterArgs& a, unsigned long l
   }
 }
 
-__device__ __forceinline__ long long unweight_word(const IterArgs& a, int j, double z, unsigned long long* emax,
-                                                   unsigned* fl) {
+__device__ __forceinline__ long long round_word(double x, int span, unsigned long long* emax, unsigned* fl) {
   unsigned long long e;
   int big = 0;
-  const double x = z * __ldg(a.Ainv + j);
-  long long r = round_ll_bits(x, &e, &big);
-  if (j == 0) r -= 2;  // the -2 of the LL step; exact on the rounded integer
+  const long long r = round_ll_bits(x, &e, &big);
   *emax = e > *emax ? e : *emax;
-  const int span = slice_span(a, j);
   const unsigned long long mag = (unsigned long long)(r < 0 ? -r : r);
   if (big) *fl |= kStatusBig;
   if (span < 63 && (mag >> span) != 0ull) *fl |= kStatusSlice;
   return r;
 }
 
-__global__ void __launch_bounds__(kMaxThreads) k_col_inv(IterArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, 2) k_col_inv(IterArgs a) {
   extern __shared__ cplx smem[];
-  const int G = a.G, H = a.H, W = a.W;
-  const int c0 = blockIdx.x * G;
-  const int ls = H;
-  cplx* buf1 = smem + G * H;
-  for (int idx = threadIdx.x; idx < G * H; idx += blockDim.x) {
-    const int l = idx % G, k2 = idx / G;
-    smem[l * ls + k2] = ldc(a.Z + k2 * W + c0 + l);
-  }
+  const int H = a.H, W = a.W;
+  const int ls = a.ls_col;
+  const int m1 = blockIdx.x;
+  cplx* buf1 = smem + ls;
+  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z + (size_t)k2 * W + m1);
   __syncthreads();
-  const cplx* res = line_fft<+1>(smem, buf1, G, ls, a.ph, a.twH);
+  const cplx* res = line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
   unsigned long long emax = 0;
   unsigned fl = 0;
-  for (int idx = threadIdx.x; idx < G * H; idx += blockDim.x) {
-    const int l = idx % G, m2 = idx / G;
-    const int j0 = 2 * (c0 + l + W * m2);
-    const cplx v = res[l * ls + m2];
-    const long long r0 = unweight_word(a, j0, v.re, &emax, &fl);
-    const long long r1 = unweight_word(a, j0 + 1, v.im, &emax, &fl);
-    *reinterpret_cast<longlong2*>(a.ll + j0) = make_longlong2(r0, r1);
+  for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
+    const int s0 = 2 * (m1 * H + m2);
+    const cplx v = res[pad(m2)];
+    const double2 ai = __ldg(reinterpret_cast<const double2*>(a.Ainv + s0));
+    const uchar2 sp = __ldg(reinterpret_cast<const uchar2*>(a.span + s0));
+    long long r0 = round_word(v.re * ai.x, sp.x, &emax, &fl);
+    const long long r1 = round_word(v.im * ai.y, sp.y, &emax, &fl);
+    if (s0 == 0) r0 -= 2;  // word 0: the -2 of the LL step, exact on the rounded integer
+    *reinterpret_cast<longlong2*>(a.ll + s0) = make_longlong2(r0, r1);
   }
   finish_status(a, emax, fl);
 }
 
+template <bool FS>
+static cudaError_t set_col_fwd_smem(int bytes) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  return cudaFuncSetAttribute(k_col_fwd<FS, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 cudaError_t set_fused_smem_limits(const FusedGeom& g) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_col))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_col))) return e;
+  if ((e = set_col_fwd_smem<false>((int)g.sm_col))) return e;
+  if ((e = set_col_fwd_smem<true>((int)g.sm_col))) return e;
   if ((e = cudaFuncSetAttribute(k_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_col))) return e;
   return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_row);
 }
 
+template <bool FS>
+static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
+  switch (a.n) {
+    case 2: k_col_fwd<FS, 2><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 3: k_col_fwd<FS, 3><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 4: k_col_fwd<FS, 4><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 5: k_col_fwd<FS, 5><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    default: k_col_fwd<FS, 6><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+  }
+}
+
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state) {
-  const int ncol = a.W / a.G;
-  if (from_state) k_col_fwd<true><<<ncol, g.t_col, g.sm_col, s>>>(a);
-  else k_col_fwd<false><<<ncol, g.t_col, g.sm_col, s>>>(a);
+  if (from_state) launch_col_fwd<true>(a, g, s);
+  else launch_col_fwd<false>(a, g, s);
   k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
-  k_col_inv<<<ncol, g.t_col, g.sm_col, s>>>(a);
+  k_col_inv<<<a.W, g.t_col, g.sm_col, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fused_kernel(const IterArgs& a, const FusedGeom& g, cudaStream_t s, int which) {
+  if (which == 0) launch_col_fwd<false>(a, g, s);
+  else if (which == 1) k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+  else k_col_inv<<<a.W, g.t_col, g.sm_col, s>>>(a);
+  return cudaGetLastError();
+}
+
+// natural <-> column-major copy of an int64 word array
+__global__ void k_permute_words(IterArgs a, const long long* __restrict__ src, long long* __restrict__ dst,
+                                bool to_colmajor) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.N) return;
+  const int c = colmajor(a, j);
+  if (to_colmajor) dst[c] = src[j];
+  else dst[j] = src[c];
+}
+
+cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
+                                 cudaStream_t s) {
+  k_permute_words<<<(a.N + 255) / 256, 256, 0, s>>>(a, src, dst, to_colmajor);
+  return cudaGetLastError();
+}
+
+// llintToIrrBal<n> over column-major products (fused form), natural-order output
+__global__ void k_dice_perm(IterArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.N) return;
+  const int N = a.N;
+  const uint32_t f = a.flags[colmajor(a, j)];
+  const long long s = dice_sum(a.LO, a.n, f, [&](int i) {
+    const int k = j - i;
+    return a.ll[colmajor(a, k < 0 ? k + N : k)];
+  });
+  int d, h;
+  balanced_split(s, a.LO + (int)(f & 1), &d, &h);
+  a.digit[j] = d;
+  a.hi[j] = (signed char)h;
+}
+
+cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s) {
+  k_dice_perm<<<(a.N + 255) / 256, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

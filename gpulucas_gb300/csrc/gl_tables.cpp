@@ -168,6 +168,17 @@ void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
   for (int64_t t = 0; t < L; ++t) tw[t] = twiddle(t, L);
 }
 
+void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw) {
+  tw.assign(L > 0 ? L : 1, HostCplx{1.0, 0.0});
+  int Ns = 1;
+  for (int R : radices) {
+    const int tws = L / (Ns * R);
+    for (int q = 1; q < R; ++q)
+      for (int k = 0; k < Ns; ++k) tw[(Ns - 1) + (q - 1) * Ns + k] = twiddle((int64_t)k * q * tws, L);
+    Ns *= R;
+  }
+}
+
 std::vector<int> radix_plan(int n, int max_radix) {
   std::vector<int> r;
   if (n <= 0) return r;

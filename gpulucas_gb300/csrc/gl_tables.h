@@ -28,6 +28,12 @@ void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, s
 void twiddle_table(int64_t L, std::vector<HostCplx>& tw);
 HostCplx twiddle(int64_t t, int64_t L);
 
+// Stage-ordered twiddles of one Stockham line DFT of length L with the given radix
+// sequence: stage s (span Ns, radix R) uses w_L^(k q L/(Ns R)) for q in [1, R),
+// k in [0, Ns), stored at (Ns - 1) + (q - 1) Ns + k, so lanes with consecutive k read
+// consecutive entries.  L - 1 entries in total (one extra slot is kept).
+void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw);
+
 // factor n into the allowed radices (16, 8, 4, 2, 3, 5, 7), largest first; empty if
 // n has another prime factor.
 std::vector<int> radix_plan(int n, int max_radix);

@@ -112,6 +112,10 @@ int gl_enqueue(gl_plan* plan, int64_t iters);
 int gl_sync_status(gl_plan* plan, gl_iter_report* report);
 /* kernel launches one iteration issues (3 for the fused form) */
 int gl_launches_per_iteration(const gl_plan* plan);
+/* Fused form only: run `iters` iterations launching each kernel between CUDA events
+ * on the plan's stream; ms_out[i] = average ms of kernel i (k_col_fwd, k_row_sq,
+ * k_col_inv); names (may be NULL) receives their names, *nk the count. */
+int gl_profile_kernels(gl_plan* plan, int iters, double* ms_out, const char** names, int* nk);
 
 /* The state after the last iteration. */
 int gl_get_products(gl_plan* plan, int64_t* ll_out);                     /* llint_signal, N int64 */
