@@ -30,22 +30,41 @@ def nvcc() -> str:
 
 
 def common_flags() -> list[str]:
-    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall",
-            "-I", os.path.join(HERE, "..", "include")] + ARCH
+    # every nvcc warning is an error: a host function reached from device code (for
+    # instance a plain constexpr helper) compiles to undefined device behaviour
+    return ["-O3", "-std=c++17", "-lineinfo", "-Werror", "all-warnings", "-Xcompiler",
+            "-fPIC,-ffp-contract=off,-Wall,-Wno-unknown-pragmas", "-I", os.path.join(HERE, "..", "include")] + ARCH
+
+
+def _check_ptxas(src: str, report: str) -> None:
+    """Every kernel must keep its arrays in registers: a stack frame or a spill means a
+    dynamically indexed array or register overflow, both a large slowdown."""
+    bad = []
+    func = None
+    for line in report.splitlines():
+        if "Compiling entry function" in line or "Function properties for" in line:
+            func = line.split("'")[1] if "'" in line else line.split()[-1]
+        if "bytes stack frame" in line:
+            parts = line.split()
+            stack, spill_st, spill_ld = int(parts[0]), int(parts[4]), int(parts[8])
+            if stack or spill_st or spill_ld:
+                bad.append(f"{func}: {line.strip()}")
+    if bad:
+        raise RuntimeError(f"{src}: kernels use local memory:\n" + "\n".join(bad))
 
 
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc()] + common_flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cu"):
-        cmd = [nvcc(), "-x", "cu"] + common_flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
-        if verbose_ptxas:
-            cmd += ["-Xptxas", "-v"]
+        cmd = [nvcc(), "-x", "cu"] + common_flags() + ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
-    if verbose_ptxas and r.stderr:
-        sys.stderr.write(r.stderr)
+    if src.endswith(".cu"):
+        _check_ptxas(src, r.stderr)
+        if verbose_ptxas:
+            sys.stderr.write(r.stderr)
     return obj
 
 
@@ -66,7 +85,8 @@ def build_hostcheck() -> str:
     """Host-only build of the device arithmetic helpers, for the CPU test suite."""
     os.makedirs(BUILD, exist_ok=True)
     tmp = HOSTCHECK + ".tmp"
-    cmd = [nvcc(), "-x", "cu", "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    cmd = [nvcc(), "-x", "cu", "-O2", "-std=c++17", "-shared", "-Werror", "all-warnings", "-Xcompiler",
+           "-fPIC,-ffp-contract=off,-Wno-unknown-pragmas",
            os.path.join(CSRC, "gl_hostcheck.cu"), os.path.join(CSRC, "gl_tables.cpp"), "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

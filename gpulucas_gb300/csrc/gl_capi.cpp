@@ -364,7 +364,9 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   std::vector<double> A, Ainv;
   std::vector<HostCplx> twM;
   word_tables(p, N, bits, flags);
-  weight_tables(p, N, 2.0 * N, A, Ainv);
+  // the row pass produces V = DFT_M(z_even + i z_odd) exactly, so the unnormalized
+  // inverse returns M z: Ainv = 1/(M A) (the reference's (1/A)/N with N = 2M)
+  weight_tables(p, N, (double)M, A, Ainv);
   twiddle_table(M, twM);
 
   IterArgs& a = pl->args;
@@ -386,9 +388,13 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   GL_TRY(dev_alloc(pl, &hi, N));
   GL_TRY(dev_alloc(pl, &status, 1));
   if (o.mode == GL_MODE_PLAIN) {
+    std::vector<HostCplx> pc((size_t)M);
+    for (int k = 0; k < M; ++k) pc[k] = pair_coeff(k, M);
     GL_TRY(dev_alloc(pl, &Z2, M));
     GL_TRY(dev_alloc(pl, &dtwM, M));
+    GL_TRY(dev_alloc(pl, &dPair, M));
     GL_TRYC(cudaMemcpy(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpy(dPair, pc.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
     GL_TRYC(cudaMemcpy(fl, flags.data(), N, cudaMemcpyHostToDevice));
     GL_TRYC(cudaMemcpy(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
     GL_TRYC(cudaMemcpy(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
@@ -409,15 +415,16 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
     }
     std::vector<int> rw(fg.pw.radix, fg.pw.radix + fg.pw.nst), rh(fg.ph.radix, fg.ph.radix + fg.ph.nst);
     std::vector<HostCplx> twW, twH, tK1((size_t)M), tPair((size_t)M), tK2((size_t)M);
-    stage_twiddles(W, rw, twW);
-    stage_twiddles(H, rh, twH);
+    stage_twiddles(W, rw, twW, fg.pw.off);
+    stage_twiddles(H, rh, twH, fg.ph.off);
     for (int k2 = 0; k2 < H; ++k2)
       for (int m1 = 0; m1 < W; ++m1) {
         const HostCplx w = twM[(size_t)m1 * k2];   // m1 * k2 < M
         tK1[(size_t)m1 * H + k2] = w;
         tK2[(size_t)k2 * W + m1] = w;
-        tPair[(size_t)k2 * W + m1] = twM[(size_t)k2 + (size_t)H * m1];
+        tPair[(size_t)k2 * W + m1] = pair_coeff((int64_t)k2 + (int64_t)H * m1, M);
       }
+    pl->fg = fg;
     GL_TRY(dev_alloc(pl, &span, N));
     GL_TRY(dev_alloc(pl, &dtwW, twW.size()));
     GL_TRY(dev_alloc(pl, &dtwH, twH.size()));
@@ -433,7 +440,7 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
     GL_TRYC(cudaMemcpy(dK1, tK1.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
     GL_TRYC(cudaMemcpy(dPair, tPair.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
     GL_TRYC(cudaMemcpy(dK2, tK2.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-    a.W = W; a.H = H; a.G = 1; a.pw = fg.pw; a.ph = fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
+    a.W = W; a.H = H; a.G = 1; a.pw = pl->fg.pw; a.ph = pl->fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
     GL_TRYC(set_fused_smem_limits(fg));
   }
   a.ll = ll; a.flags = fl; a.span = span; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;

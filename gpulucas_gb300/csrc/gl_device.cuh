@@ -225,6 +225,110 @@ GL_HD void dft7(cplx* x) {
   x[4] = mk(a3.re + b3.im, a3.im - b3.re);
 }
 
+// ---------------------------------------------------------------------------
+// Layered radix-2 DIT of R = 2^r points with an external twiddle (Linzer-Feig
+// style FMA merging).  y_p = sum_q x_q (w W_R^p)^q with W_R = exp(S 2 pi i/R):
+// after the bit-reversed input order, level l (sub-DFT size 2^l) combines
+// (a, c) -> (a + t c, a - t c) with t = w^(R/2^l) W_(2^l)^p.  For p in the upper
+// quarter t is S i times the value for p - 2^(l-2), so a level stores only
+// max(1, 2^(l-2)) values.  a + t c costs 4 FMA and a - t c = 2a - (a + t c) 2 more;
+// with t = 1 or S i a butterfly is 4 adds.
+// ---------------------------------------------------------------------------
+// (a, c) -> (a + c, a - c)
+GL_HD void bf_one(cplx& a, cplx& c) {
+  const cplx u = add(a, c);
+  c = sub(a, c);
+  a = u;
+}
+// (a, c) -> (a + S i c, a - S i c)
+template <int S>
+GL_HD void bf_si(cplx& a, cplx& c) {
+  const cplx sc = mul_si<S>(c);
+  const cplx u = add(a, sc);
+  c = sub(a, sc);
+  a = u;
+}
+// (a, c) -> (a + t c, a - t c)
+GL_HD void bf_tw(cplx& a, cplx& c, const cplx t) {
+  const double ur = fma(t.re, c.re, fma(-t.im, c.im, a.re));
+  const double ui = fma(t.re, c.im, fma(t.im, c.re, a.im));
+  c = mk(fma(2.0, a.re, -ur), fma(2.0, a.im, -ui));
+  a = mk(ur, ui);
+}
+// (a, c) -> (a + S i t c, a - S i t c)
+template <int S>
+GL_HD void bf_si_tw(cplx& a, cplx& c, const cplx t) {
+  // S i t c = S i (tr cr - ti ci) - S (tr ci + ti cr)
+  const double ur = fma(-S * t.re, c.im, fma(-S * t.im, c.re, a.re));
+  const double ui = fma(S * t.re, c.re, fma(-S * t.im, c.im, a.im));
+  c = mk(fma(2.0, a.re, -ur), fma(2.0, a.im, -ui));
+  a = mk(ur, ui);
+}
+
+__host__ __device__ constexpr int ilog2c(int r) { return r <= 1 ? 0 : 1 + ilog2c(r >> 1); }
+// reverse the low `bits` (<= 4) bits of i; plain arithmetic, so an unrolled loop index
+// folds it to a constant and the register arrays stay statically indexed
+GL_HD int bitrev4(int i, int bits) {
+  const int x = ((i & 1) << 3) | ((i & 2) << 1) | ((i & 4) >> 1) | ((i & 8) >> 3);
+  return x >> (4 - bits);
+}
+
+// exp(S 2 pi i p / size) for the constant (first-stage) twiddles, size in {8, 16}
+template <int S>
+GL_HD cplx wconst(int p, int size) {
+  // only called with p < size/4 (the S i symmetry covers the rest)
+  if (size == 8) return mk(GL_SQRT1_2, S * GL_SQRT1_2);  // p == 1
+  // size 16: p = 1, 2, 3
+  if (p == 1) return mk(GL_C8, S * GL_S8);
+  if (p == 2) return mk(GL_SQRT1_2, S * GL_SQRT1_2);
+  return mk(GL_S8, S * GL_C8);
+}
+
+// One level (sub-DFT size 2^LV) of the layered DIT; every trip count is a
+// compile-time constant so the register arrays stay statically indexed.
+template <int R, int S, bool TW, int LV>
+GL_HD void dit_level(cplx* y, const cplx* tv) {
+  constexpr int half = 1 << (LV - 1);
+  constexpr int quarter = half >> 1;
+  constexpr int vbase = LV == 1 ? 0 : (1 << (LV - 2));
+#pragma unroll
+  for (int b = 0; b < R; b += 2 * half) {
+#pragma unroll
+    for (int p = 0; p < half; ++p) {
+      const bool si = LV >= 2 && p >= quarter;
+      const int pp = si ? p - quarter : p;
+      if (TW) {
+        const cplx t = tv[vbase + pp];
+        if (si) bf_si_tw<S>(y[b + p], y[b + p + half], t);
+        else bf_tw(y[b + p], y[b + p + half], t);
+      } else if (pp == 0) {
+        if (si) bf_si<S>(y[b + p], y[b + p + half]);
+        else bf_one(y[b + p], y[b + p + half]);
+      } else {
+        const cplx t = wconst<S>(pp, 2 * half);
+        if (si) bf_si_tw<S>(y[b + p], y[b + p + half], t);
+        else bf_tw(y[b + p], y[b + p + half], t);
+      }
+    }
+  }
+}
+
+// TW = false: no external twiddle (constant W factors only).  TW = true: tv holds the
+// stage's stored values (already conjugated for S = +1).
+template <int R, int S, bool TW>
+GL_HD void layered_dit(cplx* x, const cplx* tv) {
+  constexpr int r = ilog2c(R);
+  cplx y[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) y[i] = x[bitrev4(i, r)];
+  dit_level<R, S, TW, 1>(y, tv);
+  if constexpr (R >= 4) dit_level<R, S, TW, 2>(y, tv);
+  if constexpr (R >= 8) dit_level<R, S, TW, 3>(y, tv);
+  if constexpr (R >= 16) dit_level<R, S, TW, 4>(y, tv);
+#pragma unroll
+  for (int i = 0; i < R; ++i) x[i] = y[i];
+}
+
 template <int R, int S>
 GL_HD void dft(cplx* x) {
   if constexpr (R == 2) dft2<S>(x);

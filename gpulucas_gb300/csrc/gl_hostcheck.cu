@@ -40,11 +40,17 @@ long long hc_round(double x, unsigned long long* err64, int* big) {
 double hc_dbl_from_int(int v) { return dbl_from_int(v); }
 
 // dice one word j from products ll (cyclic, length N) with flags
-long long hc_dice_sum(int LO, int n, unsigned f, const long long* ll, int N, int j) {
-  return dice_sum(LO, n, f, [&](int i) {
-    int k = j - i;
+struct CyclicProducts {
+  const long long* ll;
+  int N, j;
+  __host__ __device__ long long operator()(int i) const {
+    const int k = j - i;
     return ll[k < 0 ? k + N : k];
-  });
+  }
+};
+
+long long hc_dice_sum(int LO, int n, unsigned f, const long long* ll, int N, int j) {
+  return dice_sum(LO, n, f, CyclicProducts{ll, N, j});
 }
 
 void hc_balanced_split(long long sum, int bits, int* digit, int* hi) { balanced_split(sum, bits, digit, hi); }
@@ -83,6 +89,59 @@ void hc_word_tables(int p, int N, int* bits, unsigned char* flags) {
     bits[j] = b[j];
     flags[j] = f[j];
   }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// layered radix-2^k DIT of R points (interleaved complex), external-twiddle values
+// tv (R/2 complex, or 1 for R = 2) when with_tw, else the constant first-stage form
+int hc_layered(int R, int sign, int with_tw, const double* tv, double* xy) {
+  cplx* x = reinterpret_cast<cplx*>(xy);
+  const cplx* t = reinterpret_cast<const cplx*>(tv);
+  if (sign < 0) {
+    switch (R) {
+      case 2: with_tw ? layered_dit<2, -1, true>(x, t) : layered_dit<2, -1, false>(x, t); break;
+      case 4: with_tw ? layered_dit<4, -1, true>(x, t) : layered_dit<4, -1, false>(x, t); break;
+      case 8: with_tw ? layered_dit<8, -1, true>(x, t) : layered_dit<8, -1, false>(x, t); break;
+      case 16: with_tw ? layered_dit<16, -1, true>(x, t) : layered_dit<16, -1, false>(x, t); break;
+      default: return -1;
+    }
+  } else {
+    switch (R) {
+      case 2: with_tw ? layered_dit<2, 1, true>(x, t) : layered_dit<2, 1, false>(x, t); break;
+      case 4: with_tw ? layered_dit<4, 1, true>(x, t) : layered_dit<4, 1, false>(x, t); break;
+      case 8: with_tw ? layered_dit<8, 1, true>(x, t) : layered_dit<8, 1, false>(x, t); break;
+      case 16: with_tw ? layered_dit<16, 1, true>(x, t) : layered_dit<16, 1, false>(x, t); break;
+      default: return -1;
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// the product's stage-ordered twiddle table for a line of length L (returns the size;
+// out may be NULL to query it), offsets per stage into off
+int hc_stage_twiddles(int L, const int* radices, int nst, double* out, int* off) {
+  std::vector<int> r(radices, radices + nst);
+  std::vector<gl::HostCplx> tw;
+  gl::stage_twiddles(L, r, tw, off);
+  if (out)
+    for (size_t i = 0; i < tw.size(); ++i) {
+      out[2 * i] = tw[i].re;
+      out[2 * i + 1] = tw[i].im;
+    }
+  return (int)tw.size();
+}
+
+void hc_pair_coeff(int k, int M, double* c) {
+  gl::HostCplx v = gl::pair_coeff(k, M);
+  c[0] = v.re;
+  c[1] = v.im;
 }
 
 }  // extern "C"

@@ -22,6 +22,7 @@ struct LinePlan {
   int L;
   int nst;
   int radix[8];
+  int off[8];  // offset of each stage in the stage-ordered twiddle table
 };
 
 // Round-off / range status written by the kernels, read by the host between batches.

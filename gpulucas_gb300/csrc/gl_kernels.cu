@@ -45,12 +45,16 @@ __device__ __forceinline__ void st(DevCplx* p, cplx v) {
 __device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
 
 // Stockham DIT stage, out of place (src -> dst, one barrier).  Butterfly j of a
-// line reads x[j + q L/R], twiddles by w_L^((j mod Ns) q L/(Ns R)), does DFT_R and
-// writes x[(j - j mod Ns) R + j mod Ns + q Ns].  Twiddles come from the stage-ordered
-// table: entry (Ns - 1) + (q - 1) Ns + k.
+// line reads x[j + q L/R], applies the external twiddle w^q with
+// w = w_L^((j mod Ns) L/(Ns R)), does DFT_R and writes x[(j - j mod Ns) R + j mod Ns +
+// p Ns].  Power-of-two radices run the layered FMA-merged DIT (its per-level twiddle
+// values come from the stage-ordered table at off + v Ns + k); odd radices multiply
+// by w^q from the table and run DFT_R.
 template <int R, int S>
 __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cplx* __restrict__ dst, int nlines,
                                                int ls, int L, int Ns, const DevCplx* __restrict__ tw) {
+  constexpr bool POW2 = (R & (R - 1)) == 0;
+  constexpr int NV = POW2 ? (R == 2 ? 1 : R / 2) : R - 1;
   const int LR = L / R;
   const int nb = nlines * LR;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -62,14 +66,23 @@ __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cpl
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = s[pad(j + q * LR)];
     if (Ns > 1) {
-      const DevCplx* t = tw + (Ns - 1) + k;
+      cplx tv[NV];
 #pragma unroll
-      for (int q = 1; q < R; ++q) {
-        const cplx w = ld(t + (q - 1) * Ns);
-        v[q] = (S < 0) ? cmul(v[q], w) : cmulc(v[q], w);
+      for (int i = 0; i < NV; ++i) {
+        const cplx t = ld(tw + (size_t)i * Ns + k);
+        tv[i] = S < 0 ? t : conj(t);
       }
+      if constexpr (POW2) {
+        layered_dit<R, S, true>(v, tv);
+      } else {
+#pragma unroll
+        for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tv[q - 1]);
+        dft<R, S>(v);
+      }
+    } else {
+      if constexpr (POW2) layered_dit<R, S, false>(v, nullptr);
+      else dft<R, S>(v);
     }
-    dft<R, S>(v);
     cplx* d = dst + l * ls;
     const int base = (j - k) * R + k;
 #pragma unroll
@@ -85,14 +98,15 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
                                           const DevCplx* tw) {
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
+    const DevCplx* st = tw + lp.off[s];
     switch (lp.radix[s]) {
-      case 16: stockham_stage<16, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      case 3: stockham_stage<3, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      case 5: stockham_stage<5, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
-      default: stockham_stage<7, S>(a, b, nlines, ls, lp.L, Ns, tw); break;
+      case 16: stockham_stage<16, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      case 3: stockham_stage<3, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      case 5: stockham_stage<5, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      default: stockham_stage<7, S>(a, b, nlines, ls, lp.L, Ns, st); break;
     }
     Ns *= lp.radix[s];
     cplx* t = a;
@@ -102,21 +116,18 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
   return a;
 }
 
-// Real-signal split and square for one frequency pair (k, M-k):
-// e = U + conj(U'), o = -i (U - conj(U')), w = w_M^k;
-// V_k = e^2 + w o^2 + 2i e o ;  V_{M-k} = conj(e^2 + w o^2) + 2i conj(e o).
-// V is 4x the DFT of (z_even + i z_odd) of the squared real signal z.
-__device__ __forceinline__ void pair_square(cplx u, cplx up, cplx w, cplx* vk, cplx* vkp) {
-  const cplx e = mk(u.re + up.re, u.im - up.im);
+// Real-signal split and square for one frequency pair (k, M-k).  With U the DFT of
+// u[m] = x[2m] + i x[2m+1], E/O the DFTs of the even/odd words, E + iO = U_k, so the
+// DFT of (z_even + i z_odd) of the squared signal is
+//   V_k = E^2 + w O^2 + 2i E O = U_k^2 + (1 + w) O^2 = U_k^2 + c_k D^2,
+// D = U_k - conj(U_{M-k}), c_k = -(1 + w_M^k)/4 (from the table), and
+//   V_{M-k} = U_{M-k}^2 + conj(c_k D^2).   19 FP64 instructions per pair.
+__device__ __forceinline__ void pair_square(cplx u, cplx up, cplx c, cplx* vk, cplx* vkp) {
   const cplx d = mk(u.re - up.re, u.im + up.im);
-  const cplx o = mk(d.im, -d.re);
-  const cplx e2 = mk(fma(e.re, e.re, -e.im * e.im), 2.0 * e.re * e.im);
-  const cplx o2 = mk(fma(o.re, o.re, -o.im * o.im), 2.0 * o.re * o.im);
-  const cplx q = cmul(o2, w);
-  const cplx r = cmul(e, o);
-  const double pr = e2.re + q.re, pi = e2.im + q.im;
-  *vk = mk(fma(-2.0, r.im, pr), fma(2.0, r.re, pi));
-  *vkp = mk(fma(2.0, r.im, pr), fma(2.0, r.re, -pi));
+  const cplx d2 = mk(fma(d.re, d.re, -d.im * d.im), 2.0 * d.re * d.im);
+  const cplx pc = cmul(c, d2);
+  *vk = mk(fma(u.re, u.re, fma(-u.im, u.im, pc.re)), fma(2.0 * u.re, u.im, pc.im));
+  *vkp = mk(fma(up.re, up.re, fma(-up.im, up.im, pc.re)), fma(2.0 * up.re, up.im, -pc.im));
 }
 
 // column-major position of natural word j (fused form layout)
@@ -434,12 +445,12 @@ __global__ void k_plain_stage(const DevCplx* __restrict__ x, DevCplx* __restrict
 }
 
 // ComplexPointwiseSqr (gpuLucas.cu:647-665) with the real-signal split: pairs (k, M-k)
-__global__ void k_plain_pair_square(DevCplx* Z, const DevCplx* __restrict__ twM, int M) {
+__global__ void k_plain_pair_square(DevCplx* Z, const DevCplx* __restrict__ pairC, int M) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k > M / 2) return;
   const int kp = k == 0 ? 0 : M - k;
   cplx vk, vkp;
-  pair_square(ldc(Z + k), ldc(Z + kp), ld(twM + k), &vk, &vkp);
+  pair_square(ldc(Z + k), ldc(Z + kp), ld(pairC + k), &vk, &vkp);
   st(Z + k, vk);
   if (kp != k) st(Z + kp, vkp);
 }
@@ -507,7 +518,7 @@ cudaError_t launch_plain_iteration(const IterArgs& a, const PlainGeom& g, cudaSt
   DevCplx* src = a.Z;
   DevCplx* dst = a.Z2;
   plain_fft<-1>(a, g, src, dst, s);
-  k_plain_pair_square<<<(a.M / 2 + 1 + T - 1) / T, T, 0, s>>>(src, a.twM, a.M);
+  k_plain_pair_square<<<(a.M / 2 + 1 + T - 1) / T, T, 0, s>>>(src, a.twPair, a.M);
   plain_fft<+1>(a, g, src, dst, s);
   k_plain_unweight<<<(a.N + T - 1) / T, T, 0, s>>>(a, reinterpret_cast<const double*>(src));
   k_dice<<<(a.N + T - 1) / T, T, 0, s>>>(a);

@@ -140,7 +140,9 @@ void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, s
   }
 }
 
-HostCplx twiddle(int64_t t, int64_t L) {
+namespace {
+// cos and sin of 2 pi t / L in double-double
+void cos_sin_dd(int64_t t, int64_t L, DD* C, DD* S) {
   t %= L;
   if (t < 0) t += L;
   int64_t u = 8 * t;
@@ -149,18 +151,31 @@ HostCplx twiddle(int64_t t, int64_t L) {
   DD s, c;
   if (o & 1) sincos_octant(L - r, L, &s, &c);
   else sincos_octant(r, L, &s, &c);
-  double cs = to_double(c), sn = to_double(s), C, S;
   switch (o) {
-    case 0: C = cs; S = sn; break;
-    case 1: C = sn; S = cs; break;
-    case 2: C = -sn; S = cs; break;
-    case 3: C = -cs; S = sn; break;
-    case 4: C = -cs; S = -sn; break;
-    case 5: C = -sn; S = -cs; break;
-    case 6: C = sn; S = -cs; break;
-    default: C = cs; S = -sn; break;
+    case 0: *C = c; *S = s; break;
+    case 1: *C = s; *S = c; break;
+    case 2: *C = -s; *S = c; break;
+    case 3: *C = -c; *S = s; break;
+    case 4: *C = -c; *S = -s; break;
+    case 5: *C = -s; *S = -c; break;
+    case 6: *C = s; *S = -c; break;
+    default: *C = c; *S = -s; break;
   }
-  return {C, -S};
+}
+}  // namespace
+
+HostCplx twiddle(int64_t t, int64_t L) {
+  DD C, S;
+  cos_sin_dd(t, L, &C, &S);
+  return {to_double(C), -to_double(S)};
+}
+
+HostCplx pair_coeff(int64_t k, int64_t M) {
+  DD C, S;
+  cos_sin_dd(k, M, &C, &S);
+  // -(1 + cos - i sin)/4
+  DD re = dd(1.0) + C;
+  return {-0.25 * to_double(re), 0.25 * to_double(S)};
 }
 
 void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
@@ -168,13 +183,46 @@ void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
   for (int64_t t = 0; t < L; ++t) tw[t] = twiddle(t, L);
 }
 
-void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw) {
-  tw.assign(L > 0 ? L : 1, HostCplx{1.0, 0.0});
+int stage_values(int R) {
+  switch (R) {
+    case 2: return 1;
+    case 4: return 2;
+    case 8: return 4;
+    case 16: return 8;
+    default: return R - 1;
+  }
+}
+
+void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw, int* off) {
+  std::vector<HostCplx> base;
+  twiddle_table(L, base);
+  tw.assign(1, HostCplx{1.0, 0.0});
   int Ns = 1;
-  for (int R : radices) {
-    const int tws = L / (Ns * R);
-    for (int q = 1; q < R; ++q)
-      for (int k = 0; k < Ns; ++k) tw[(Ns - 1) + (q - 1) * Ns + k] = twiddle((int64_t)k * q * tws, L);
+  for (size_t s = 0; s < radices.size(); ++s) {
+    const int R = radices[s];
+    off[s] = (int)tw.size();
+    if (Ns > 1) {
+      const int tws = L / (Ns * R);
+      const int nv = stage_values(R);
+      const size_t start = tw.size();
+      tw.resize(start + (size_t)nv * Ns);
+      for (int k = 0; k < Ns; ++k) {
+        const int64_t e = (int64_t)k * tws;  // exponent of w = w_L^e
+        if (R & (R - 1)) {
+          for (int q = 1; q < R; ++q) tw[start + (size_t)(q - 1) * Ns + k] = base[(e * q) % L];
+        } else {
+          int v = 0;
+          for (int l = 1; (1 << l) <= R; ++l) {
+            const int np = l == 1 ? 1 : (1 << (l - 2));
+            for (int p = 0; p < np; ++p, ++v) {
+              // w^(R/2^l) * W_(2^l)^p = w_L^(e R/2^l + p L/2^l)
+              const int64_t idx = (e * (R >> l) + (int64_t)p * (L >> l)) % L;
+              tw[start + (size_t)v * Ns + k] = base[idx];
+            }
+          }
+        }
+      }
+    }
     Ns *= R;
   }
 }

@@ -29,10 +29,22 @@ void twiddle_table(int64_t L, std::vector<HostCplx>& tw);
 HostCplx twiddle(int64_t t, int64_t L);
 
 // Stage-ordered twiddles of one Stockham line DFT of length L with the given radix
-// sequence: stage s (span Ns, radix R) uses w_L^(k q L/(Ns R)) for q in [1, R),
-// k in [0, Ns), stored at (Ns - 1) + (q - 1) Ns + k, so lanes with consecutive k read
-// consecutive entries.  L - 1 entries in total (one extra slot is kept).
-void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw);
+// sequence.  Stage s (span Ns, radix R, external twiddle w = w_L^(k L/(Ns R)) for
+// butterfly position k < Ns) stores its values v-major at off[s] + v*Ns + k, so lanes
+// with consecutive k read consecutive entries:
+//  - R a power of two: the layered radix-2 DIT needs, at level l = 1..log2 R, the
+//    values w^(R/2^l) * W_(2^l)^p for p < max(1, 2^(l-2)) (the other half are the same
+//    times +-i): v runs over (l=1,p=0), (l=2,p=0), (l=3,p=0..1), (l=4,p=0..3);
+//  - R odd: w^q for q = 1..R-1.
+// The first stage (Ns = 1) needs no table.  Returns the table (at least one entry)
+// and fills off[] (offset of each stage).
+void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw, int* off);
+// number of stored values per butterfly position for a stage of radix R
+int stage_values(int R);
+
+// -(1 + w_M^k)/4 from double-double cos/sin, rounded once: the coefficient of the
+// real-signal square V_k = U_k^2 + c_k (U_k - conj(U_{M-k}))^2.
+HostCplx pair_coeff(int64_t k, int64_t M);
 
 // factor n into the allowed radices (16, 8, 4, 2, 3, 5, 7), largest first; empty if
 // n has another prime factor.

@@ -90,3 +90,43 @@ def test_dice_matches_oracle(hc, orc):
             h = ctypes.c_int()
             hc.hc_balanced_split(s, LO + int(flags[j] & 1), ctypes.byref(d), ctypes.byref(h))
             assert (d.value, h.value) == (int(d_ref[j]), int(h_ref[j])), (p, N, j)
+
+
+def _level_values(R, w, sign):
+    """Stored per-level twiddle values of the layered DIT: w^(R/2^l) W_(2^l)^p for
+    p < max(1, 2^(l-2)), W = exp(-2 pi i/size) (conjugated for the inverse)."""
+    vals = []
+    l = 1
+    while (1 << l) <= R:
+        n_p = 1 if l == 1 else 1 << (l - 2)
+        for p in range(n_p):
+            vals.append(w ** (R >> l) * np.exp(-2j * np.pi * p / (1 << l)))
+        l += 1
+    vals = np.array(vals)
+    return vals if sign < 0 else np.conj(vals)
+
+
+@pytest.mark.parametrize("R", [2, 4, 8, 16])
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("with_tw", [0, 1])
+def test_layered_dit(hc, R, sign, with_tw):
+    hc.hc_layered.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
+                              np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+    hc.hc_layered.restype = ctypes.c_int
+    rng = np.random.default_rng(100 * R + 10 * with_tw + sign)
+    for _ in range(20):
+        x = rng.standard_normal(R) + 1j * rng.standard_normal(R)
+        k, L = int(rng.integers(0, 256)), 1024
+        w = np.exp(-2j * np.pi * k / L) if with_tw else 1.0
+        tv = _level_values(R, w, sign)
+        tbuf = np.empty(2 * len(tv))
+        tbuf[0::2], tbuf[1::2] = tv.real, tv.imag
+        buf = np.empty(2 * R)
+        buf[0::2], buf[1::2] = x.real, x.imag
+        assert hc.hc_layered(R, sign, with_tw, tbuf, buf) == 0
+        y = buf[0::2] + 1j * buf[1::2]
+        ww = w if sign < 0 else np.conj(w)
+        xt = x * ww ** np.arange(R)
+        ref = np.fft.fft(xt) if sign < 0 else np.fft.ifft(xt) * R
+        assert np.abs(y - ref).max() <= 1e-14 * max(1.0, np.abs(ref).max())
