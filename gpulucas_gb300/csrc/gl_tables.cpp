@@ -126,18 +126,18 @@ void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>&
   }
 }
 
+void weight_entry(int p, int N, int j, double inv_scale_den, double* A, double* Ainv) {
+  // ceil(jp/N) - jp/N = r/N with r = ceil(jp/N)*N - jp, an exact integer
+  const int64_t r = ceil_div_pos((int64_t)p * j, N) * N - (int64_t)p * j;
+  const DD e = exp_small((dd((double)r) / dd((double)N)) * kLn2);
+  *A = to_double(e);
+  *Ainv = to_double((dd(1.0) / e) / dd(inv_scale_den));
+}
+
 void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, std::vector<double>& Ainv) {
   A.resize(N);
   Ainv.resize(N);
-  const DD dN = dd((double)N);
-  const DD den = dd(inv_scale_den);
-  for (int j = 0; j < N; ++j) {
-    // ceil(jp/N) - jp/N = r/N with r = ceil(jp/N)*N - jp, an exact integer
-    int64_t r = ceil_div_pos((int64_t)p * j, N) * N - (int64_t)p * j;
-    DD e = exp_small((dd((double)r) / dN) * kLn2);
-    A[j] = to_double(e);
-    Ainv[j] = to_double((dd(1.0) / e) / den);
-  }
+  for (int j = 0; j < N; ++j) weight_entry(p, N, j, inv_scale_den, &A[j], &Ainv[j]);
 }
 
 namespace {

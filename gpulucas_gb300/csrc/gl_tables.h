@@ -24,6 +24,9 @@ void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>&
 // scale = 1/N; the fused kernels need 1/(2N)).
 void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, std::vector<double>& Ainv);
 
+// One entry of weight_tables: A[j] and Ainv[j] (same rounding), no containers.
+void weight_entry(int p, int N, int j, double inv_scale_den, double* A, double* Ainv);
+
 // exp(-2 pi i t / L) for t in [0, L), correctly rounded from double-double.
 void twiddle_table(int64_t L, std::vector<HostCplx>& tw);
 HostCplx twiddle(int64_t t, int64_t L);
