@@ -32,6 +32,8 @@ GL_ERR_NODEVICE = -8
 GL_ERR_IO = -9
 GL_ERR_CHECKPOINT = -10
 GL_ERR_STATE = -11
+GL_ERR_TOO_LARGE = -12
+NOALLOC_MAX_N = 65536
 
 MODE_FUSED = 0
 MODE_PLAIN = 1
@@ -99,6 +101,8 @@ def _load():
         "gl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
         "gl_version": (ctypes.c_int, []),
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+        "gl_iterate_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int64,
+                                              ctypes.POINTER(ctypes.c_double), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -117,7 +121,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_get_products",
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
-    "gl_probe_fp64_peak",
+    "gl_probe_fp64_peak", "gl_iterate_noalloc",
 ]))
 
 
@@ -279,6 +283,15 @@ def error_test(p: int, N: int, iters: int = 0, **opts) -> IterReport:
     o = default_opts(**opts)
     _check(lib.gl_error_test(int(p), int(N), ctypes.byref(o), int(iters), ctypes.byref(rep)), "error_test")
     return rep
+
+
+def iterate_noalloc(p: int, N: int, ll_in_ptr: int, ll_out_ptr: int, iters: int, stream: int = 0) -> float:
+    """LL iterations on caller-owned device products without any device allocation
+    (see gl_iterate_noalloc in include/gpulucas.h); returns the max round-off."""
+    err = ctypes.c_double()
+    _check(lib.gl_iterate_noalloc(int(p), int(N), ctypes.c_void_p(ll_in_ptr), ctypes.c_void_p(ll_out_ptr),
+                                  int(iters), ctypes.byref(err), ctypes.c_void_p(stream)), "iterate_noalloc")
+    return err.value
 
 
 def probe_fp64_peak(device: int = 0, ms: float = 200.0) -> float:

@@ -292,6 +292,7 @@ const char* gl_error_string(int s) {
     case GL_ERR_IO: return "checkpoint I/O error";
     case GL_ERR_CHECKPOINT: return "checkpoint does not match the test";
     case GL_ERR_STATE: return "call not valid in this state";
+    case GL_ERR_TOO_LARGE: return "N exceeds 65536, the limit of gl_iterate_noalloc";
     default: return "unknown status";
   }
 }

@@ -35,6 +35,7 @@ extern "C" {
 #define GL_ERR_IO -9         /* checkpoint file could not be read or written */
 #define GL_ERR_CHECKPOINT -10 /* checkpoint does not match this test */
 #define GL_ERR_STATE -11     /* call not valid in the plan's current state */
+#define GL_ERR_TOO_LARGE -12 /* N above the limit of the no-allocation entry point */
 
 /* execution forms */
 #define GL_MODE_FUSED 0      /* 3 fused kernels per iteration (the product form) */
@@ -148,6 +149,24 @@ int setSliceAndDice(int testPrime, int signalSize);
 /* Plan-based forms with full results. */
 int gl_error_test(int p, int N, const gl_plan_opts* opts, int iters, gl_iter_report* report);
 int gl_mersenne_test(gl_plan* plan, int64_t iters, gl_result* result);
+
+/* --- no device allocation ------------------------------------------------ */
+
+/* No counterpart in the reference.  For callers that may not call cudaMalloc (a
+ * framework memory pool owns the device, or allocation would stall shared work):
+ * runs `iters` LL iterations (the plain form, bit-identical products to a
+ * GL_MODE_PLAIN plan) on the current device and `stream` (NULL = default stream),
+ * from the products ll_in to the products ll_out (N int64 each, device memory owned
+ * by the caller, natural word order; they may be the same buffer), and stores the
+ * maximum round-off in *max_roundoff.  It allocates nothing: its work arrays, tables
+ * and status word live in a static device array sized for N <= 65536 (about 3.3 MiB,
+ * held on every GPU that loads the library until exit); larger N returns
+ * GL_ERR_TOO_LARGE.  The first call on a device looks up that array's address;
+ * make it before any stream capture on that device.  All calls share the array, so
+ * calls that overlap on the GPU race; the host side is serialised by a lock.
+ * Returns GL_ERR_ROUNDOFF at round-off >= 0.4 and GL_ERR_OVERFLOW as gl_iterate. */
+int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* ll_out, int64_t iters,
+                       double* max_roundoff, void* stream);
 
 /* --- utilities ----------------------------------------------------------- */
 const char* gl_error_string(int status);
