@@ -42,7 +42,7 @@ MODE_PLAIN = 1
 class PlanOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("device", ctypes.c_int), ("error_limit", ctypes.c_double),
                 ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
-                ("cols_per_cta", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+                ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -101,6 +101,8 @@ def _load():
         "gl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
         "gl_version": (ctypes.c_int, []),
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+        "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
+                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gl_iterate_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int64,
                                               ctypes.POINTER(ctypes.c_double), vp]),
     }
@@ -121,7 +123,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_get_products",
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
-    "gl_probe_fp64_peak", "gl_iterate_noalloc",
+    "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size",
 ]))
 
 
@@ -164,6 +166,7 @@ class Plan:
         info = PlanInfo()
         _check(lib.gl_plan_get_info(self._h, ctypes.byref(info)), "plan info")
         self.info = info
+        self.N = info.N  # N = 0 asks the library to choose it
 
     # lifetime -----------------------------------------------------------------
     def close(self):
@@ -283,6 +286,17 @@ def error_test(p: int, N: int, iters: int = 0, **opts) -> IterReport:
     o = default_opts(**opts)
     _check(lib.gl_error_test(int(p), int(N), ctypes.byref(o), int(iters), ctypes.byref(rep)), "error_test")
     return rep
+
+
+def find_signal_size(p: int, **opts):
+    """(N, ms per iteration, max round-off of the trial) chosen for exponent p."""
+    N = ctypes.c_int()
+    ms = ctypes.c_double()
+    err = ctypes.c_double()
+    o = default_opts(**opts)
+    _check(lib.gl_find_signal_size(int(p), ctypes.byref(o), ctypes.byref(N), ctypes.byref(ms), ctypes.byref(err)),
+           f"find_signal_size p={p}")
+    return N.value, ms.value, err.value
 
 
 def iterate_noalloc(p: int, N: int, ll_in_ptr: int, ll_out_ptr: int, iters: int, stream: int = 0) -> float:

@@ -1,7 +1,10 @@
 // gl_capi.cpp -- the C ABI (include/gpulucas.h): plans, iteration, residues and the
 // reference-named entry points errorTest / mersenneTest / setSliceAndDice.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -58,7 +61,7 @@ int dev_alloc(gl_plan* pl, T** ptr, size_t count) {
 }
 
 bool fill_line_plan(int L, LinePlan* lp) {
-  std::vector<int> r = radix_plan(L, 16);
+  std::vector<int> r = radix_plan(L, kMaxRadix);
   if (r.empty() || r.size() > 8) return false;
   lp->L = L;
   lp->nst = (int)r.size();
@@ -68,24 +71,34 @@ bool fill_line_plan(int L, LinePlan* lp) {
 
 int round_up32(int x) { return (x + 31) / 32 * 32; }
 
-// FP64 instructions per element of one line DFT with the given radices: the DFT_R
-// kernels of gl_device.cuh plus one complex twiddle product per non-first-stage input.
+// FP64 instructions per point of one line DFT with the given radices: power-of-two
+// stages run the layered FMA-merged DIT (first stage: constant twiddles only, later
+// stages: 3 instructions per point and bit); odd radices run DFT_R plus one complex
+// twiddle product per non-first-stage input.
 double line_ops(const LinePlan& lp) {
-  auto dft_ops = [](int r) {
+  auto first_pow2 = [](int r) {
     switch (r) {
-      case 2: return 4.0;
-      case 3: return 12.0;
-      case 4: return 16.0;
+      case 2: return 2.0;
+      case 4: return 4.0;
+      case 8: return 6.5;
+      default: return 9.25;  // 16
+    }
+  };
+  auto odd_ops = [](int r) {
+    switch (r) {
+      case 3: return 14.0;
       case 5: return 36.0;
-      case 7: return 72.0;
-      case 8: return 60.0;
-      default: return 150.0;  // 16
+      default: return 72.0;  // 7
     }
   };
   double ops = 0.0;
   for (int s = 0; s < lp.nst; ++s) {
     const int r = lp.radix[s];
-    ops += dft_ops(r) / r + (s ? 4.0 * (r - 1) / r : 0.0);
+    const bool pow2 = (r & (r - 1)) == 0;
+    int lg = 0;
+    while ((1 << lg) < r) ++lg;
+    if (pow2) ops += s ? 3.0 * lg : first_pow2(r);
+    else ops += odd_ops(r) / r + (s ? 4.0 * (r - 1) / r : 0.0);
   }
   return ops;
 }
@@ -97,30 +110,37 @@ int padded_stride(int L) { return L + (L >> 4) + 1; }
 // ceil(units / sms) of them, so the modelled time is the sum over the three kernels
 // of ceil(units/sms) * FP64 instructions per unit.  Shared memory per CTA must fit
 // twice (two CTAs per SM at least) and blocks stay <= kMaxThreads.
-int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
+// Every usable column length H of M = W * H with its modelled cost, cheapest first.
+std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
   if (sms <= 0) sms = 152;
-  int bestH = 0;
-  double best = 1e300;
+  std::vector<std::pair<double, int>> out;
   for (int H = 2; H <= M / 2; ++H) {
     if (M % H) continue;
-    if (force_h && H != force_h) continue;
     const int W = M / H;
     if (W < 2) continue;
     LinePlan a, b;
     if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
     const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = (size_t)4 * padded_stride(W) * 16;
-    if (smc > 110 * 1024 || smr > 110 * 1024) continue;
-    if ((H + 15) / 16 > kMaxThreads) continue;
+    if (smc > (size_t)kMaxDynSmem || smr > (size_t)kMaxDynSmem) continue;
+    if ((H + kElemsPerThread - 1) / kElemsPerThread > 4 * kMaxThreads) continue;
     const double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
     const double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * line_ops(a) + 16.0);
     double cost = 2.0 * col + row;
     // prefer smaller shared-memory footprints (more resident CTAs) on ties
     cost *= 1.0 + 0.02 * (double)(smc + smr) / (64.0 * 1024);
-    if (cost < best) {
-      best = cost;
-      bestH = H;
-    }
+    out.emplace_back(cost, H);
   }
+  std::sort(out.begin(), out.end());
+  return out;
+}
+
+int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
+  int bestH = 0;
+  for (const auto& c : ranked_layouts(M, sms))
+    if (!force_h || c.second == force_h) {
+      bestH = c.second;
+      break;
+    }
   if (!bestH) return GL_ERR_SIZE;
   g->H = bestH;
   g->W = M / bestH;
@@ -132,7 +152,7 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
   g->sm_col = (size_t)2 * g->ls_col * 16;
   g->sm_row = (size_t)4 * g->ls_row * 16;
   auto threads = [](int points, int cap) {
-    int t = round_up32((points + 15) / 16);
+    int t = round_up32((points + kElemsPerThread - 1) / kElemsPerThread);
     return t < 64 ? 64 : (t > cap ? cap : t);
   };
   g->t_col = threads(g->H, kMaxThreads);
@@ -147,6 +167,93 @@ int choose_plain_geom(int M, PlainGeom* g) {
   for (int i = 0; i < g->nst; ++i) g->radix[i] = r[i];
   g->threads = 256;
   return GL_OK;
+}
+
+// offsets of each stage in a stage-ordered twiddle table (gl_tables.cpp layout) and
+// the table length, without computing the values
+int stage_offsets(const LinePlan& lp, int* off) {
+  int size = 1, Ns = 1;
+  for (int s = 0; s < lp.nst; ++s) {
+    off[s] = size;
+    if (Ns > 1) size += stage_values(lp.radix[s]) * Ns;
+    Ns *= lp.radix[s];
+  }
+  return size;
+}
+
+// Device time of one fused iteration with column length H, measured on zero-filled
+// buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
+double time_layout(int M, int H, int n, int sms, int iters, cudaStream_t s) {
+  FusedGeom g{};
+  if (choose_fused_geom(M, H, sms, &g) != GL_OK) return -1.0;
+  const int N = 2 * M;
+  const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
+  const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
+                          16 * (size_t)M, 16 * (size_t)M, 16 * (size_t)M, 16 * (size_t)M,
+                          16 * (size_t)szw, 16 * (size_t)szh, sizeof(int) * N, (size_t)N, sizeof(Status)};
+  constexpr int nb = sizeof(bytes) / sizeof(bytes[0]);
+  void* buf[nb] = {};
+  double ms = -1.0;
+  bool ok = true;
+  for (int i = 0; i < nb && ok; ++i) ok = cudaMalloc(&buf[i], bytes[i]) == cudaSuccess &&
+                                         cudaMemsetAsync(buf[i], 0, bytes[i], s) == cudaSuccess;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ok) ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+  if (ok) ok = set_fused_smem_limits(g) == cudaSuccess;
+  if (ok) {
+    IterArgs a{};
+    a.N = N; a.M = M; a.W = g.W; a.H = g.H; a.G = 1; a.LO = 18; a.n = n;
+    a.ls_col = g.ls_col; a.ls_row = g.ls_row; a.pw = g.pw; a.ph = g.ph;
+    a.ll = (long long*)buf[0]; a.flags = (const unsigned char*)buf[1]; a.span = (const unsigned char*)buf[2];
+    a.A = (const double*)buf[3]; a.Ainv = (const double*)buf[4]; a.Z = (DevCplx*)buf[5];
+    a.twK1 = (const DevCplx*)buf[6]; a.twPair = (const DevCplx*)buf[7]; a.twK2 = (const DevCplx*)buf[8];
+    a.twW = (const DevCplx*)buf[9]; a.twH = (const DevCplx*)buf[10];
+    a.digit = (int*)buf[11]; a.hi = (signed char*)buf[12]; a.status = (Status*)buf[13];
+    for (int i = 0; i < 2 && ok; ++i) ok = launch_fused_iteration(a, g, s, false) == cudaSuccess;
+    ok = ok && cudaEventRecord(e0, s) == cudaSuccess;
+    for (int i = 0; i < iters && ok; ++i) ok = launch_fused_iteration(a, g, s, false) == cudaSuccess;
+    ok = ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
+    float t = 0.f;
+    if (ok && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess) ms = t / iters;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(s);
+  for (void* b : buf)
+    if (b) cudaFree(b);
+  return ms;
+}
+
+// Autotuned column length for M on this device: the cheapest few layouts of the cost
+// model are timed and the fastest kept, once per (M, SM count) per process.
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, std::pair<int, double>> g_tune_cache;
+
+int autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_out) {
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find({M, sms});
+    if (it != g_tune_cache.end()) {
+      if (ms_out) *ms_out = it->second.second;
+      return it->second.first;
+    }
+  }
+  const auto ranked = ranked_layouts(M, sms);
+  int best = 0;
+  double best_ms = 1e300;
+  const int iters = M >= (1 << 18) ? 10 : 40;
+  for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
+    const double ms = time_layout(M, ranked[i].second, n, sms, iters, s);
+    if (ms > 0.0 && ms < best_ms) {
+      best_ms = ms;
+      best = ranked[i].second;
+    }
+  }
+  if (!best) return 0;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_cache[{M, sms}] = {best, best_ms};
+  if (ms_out) *ms_out = best_ms;
+  return best;
 }
 
 void free_plan(gl_plan* pl) {
@@ -305,6 +412,7 @@ int gl_default_opts(gl_plan_opts* o) {
   o->error_limit = 0.4;
   o->check_every = 1000;
   o->use_graphs = 1;
+  o->autotune = 1;
   return GL_OK;
 }
 
@@ -320,6 +428,10 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   gl_plan_opts o;
   if (opts) o = *opts;
   else gl_default_opts(&o);
+  if (N == 0 && p >= 3) {
+    int rc0 = gl_find_signal_size(p, &o, &N, nullptr, nullptr);
+    if (rc0 != GL_OK) return rc0;
+  }
   if (p < 3 || N < 16 || (N & 1) || N > p) return GL_ERR_ARG;
   if (o.mode != GL_MODE_FUSED && o.mode != GL_MODE_PLAIN) return GL_ERR_ARG;
   if (!(o.error_limit > 0.0 && o.error_limit <= 0.5) || o.check_every < 1) return GL_ERR_ARG;
@@ -335,7 +447,9 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   if (cudaSetDevice(o.device) != cudaSuccess) return GL_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess) return GL_ERR_CUDA;
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, o.fft_h, sms, &fg) : choose_plain_geom(M, &pg);
+  int force_h = o.fft_h;
+  if (o.mode == GL_MODE_FUSED && !force_h && o.autotune) force_h = autotune_layout(M, n, sms, 0, nullptr);
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg) : choose_plain_geom(M, &pg);
   if (rc != GL_OK) return rc;
 
   gl_plan* pl = new (std::nothrow) gl_plan();
@@ -390,7 +504,9 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   GL_TRY(dev_alloc(pl, &status, 1));
   if (o.mode == GL_MODE_PLAIN) {
     std::vector<HostCplx> pc((size_t)M);
-    for (int k = 0; k < M; ++k) pc[k] = pair_coeff(k, M);
+    parallel_for(M, [&](int64_t b, int64_t e) {
+      for (int64_t k = b; k < e; ++k) pc[k] = pair_coeff(k, M);
+    });
     GL_TRY(dev_alloc(pl, &Z2, M));
     GL_TRY(dev_alloc(pl, &dtwM, M));
     GL_TRY(dev_alloc(pl, &dPair, M));
@@ -418,13 +534,15 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
     std::vector<HostCplx> twW, twH, tK1((size_t)M), tPair((size_t)M), tK2((size_t)M);
     stage_twiddles(W, rw, twW, fg.pw.off);
     stage_twiddles(H, rh, twH, fg.ph.off);
-    for (int k2 = 0; k2 < H; ++k2)
-      for (int m1 = 0; m1 < W; ++m1) {
-        const HostCplx w = twM[(size_t)m1 * k2];   // m1 * k2 < M
-        tK1[(size_t)m1 * H + k2] = w;
-        tK2[(size_t)k2 * W + m1] = w;
-        tPair[(size_t)k2 * W + m1] = pair_coeff((int64_t)k2 + (int64_t)H * m1, M);
-      }
+    parallel_for(H, [&](int64_t b, int64_t e) {
+      for (int64_t k2 = b; k2 < e; ++k2)
+        for (int m1 = 0; m1 < W; ++m1) {
+          const HostCplx w = twM[(size_t)m1 * k2];   // m1 * k2 < M
+          tK1[(size_t)m1 * H + k2] = w;
+          tK2[(size_t)k2 * W + m1] = w;
+          tPair[(size_t)k2 * W + m1] = pair_coeff(k2 + (int64_t)H * m1, M);
+        }
+    });
     pl->fg = fg;
     GL_TRY(dev_alloc(pl, &span, N));
     GL_TRY(dev_alloc(pl, &dtwW, twW.size()));
@@ -768,6 +886,59 @@ int gl_error_test(int p, int N, const gl_plan_opts* opts, int iters, gl_iter_rep
   rc = gl_iterate(pl, iters, rep);
   gl_plan_destroy(pl);
   return rc;
+}
+
+int gl_find_signal_size(int p, const gl_plan_opts* opts, int* N_out, double* ms_per_iter, double* max_roundoff) {
+  if (!N_out || p < 64) return GL_ERR_ARG;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  o.mode = GL_MODE_FUSED;
+  o.fft_h = 0;
+  o.error_limit = 0.5;
+  o.check_every = 100;
+  // candidate lengths, smallest first
+  std::vector<int> cand;
+  for (int64_t p2 = 2; p2 <= (1 << 26); p2 *= 2)
+    for (int64_t p3 = 1, b = 0; b <= 5; p3 *= 3, ++b)
+      for (int64_t p5 = 1, c = 0; c <= 3; p5 *= 5, ++c)
+        for (int64_t p7 = 1, d = 0; d <= 2; p7 *= 7, ++d) {
+          const int64_t N = p2 * p3 * p5 * p7;
+          if (N < 64 || N > p / 8 || N > (1 << 27)) continue;
+          if (slice_depth(p, (int)N) < 0) continue;
+          cand.push_back((int)N);
+        }
+  std::sort(cand.begin(), cand.end());
+  cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+  int best = 0, first = 0;
+  double best_ms = 1e300, best_err = 0.0;
+  for (int N : cand) {
+    if (first && N > first + first / 7) break;  // within ~15 % of the smallest accepted
+    gl_plan* pl = nullptr;
+    int rc = gl_plan_create(p, N, &o, &pl);
+    if (rc == GL_ERR_NOMEM || rc == GL_ERR_NODEVICE || rc == GL_ERR_CUDA) return rc;
+    if (rc != GL_OK) continue;
+    gl_iter_report rep{};
+    rc = gl_iterate(pl, 100, &rep);
+    double ms = -1.0;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, pl->device);
+    autotune_layout(N / 2, pl->n, sms, 0, &ms);
+    gl_plan_destroy(pl);
+    if (rc == GL_ERR_CUDA) return rc;
+    if (rc != GL_OK || rep.max_roundoff >= 0.30 || ms <= 0.0) continue;
+    if (!first) first = N;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = N;
+      best_err = rep.max_roundoff;
+    }
+  }
+  if (!best) return GL_ERR_SIZE;
+  *N_out = best;
+  if (ms_per_iter) *ms_per_iter = best_ms;
+  if (max_roundoff) *max_roundoff = best_err;
+  return GL_OK;
 }
 
 float errorTest(int testPrime, int signalSize) {

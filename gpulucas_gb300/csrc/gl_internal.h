@@ -8,10 +8,16 @@
 
 namespace gl {
 
-// the fused kernels are compiled for at most this many threads per CTA
+// Line FFTs of the fused form use radices <= kMaxRadix and about kElemsPerThread
+// points per thread: a radix-8 butterfly keeps 8 complex values (32 registers) live,
+// so 3 CTAs of 256 threads fit an SM's registers.  With FMA-merged layered stages a
+// radix-8 stage costs the same 3 FP64 instructions per point and bit as a radix-16 one.
+constexpr int kMaxRadix = 8;
+constexpr int kElemsPerThread = 8;
 constexpr int kMaxThreads = 256;
-// the row pass (two lines, two buffers) is compiled for at most 128 threads, 3 CTAs/SM
-constexpr int kRowThreads = 128;
+constexpr int kRowThreads = 256;
+// upper bound of a fused kernel's dynamic shared memory (the layout chooser keeps below)
+constexpr int kMaxDynSmem = 112 * 1024;
 
 struct DevCplx {
   double re, im;

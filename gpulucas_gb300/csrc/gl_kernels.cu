@@ -99,8 +99,8 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
     const DevCplx* st = tw + lp.off[s];
+    static_assert(kMaxRadix == 8, "line plans use radices 2, 4, 8, 3, 5, 7");
     switch (lp.radix[s]) {
-      case 16: stockham_stage<16, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, st); break;
@@ -146,7 +146,7 @@ __device__ __forceinline__ int colmajor(const IterArgs& a, int j) {
 // j0 = 2m, j0+1 the digit sums of j0-1, j0, j0+1 need the products of words
 // j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.
 template <bool FROM_STATE, int NC>
-__global__ void __launch_bounds__(kMaxThreads, 2) k_col_fwd(IterArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
   extern __shared__ cplx smem[];
   const int H = a.H, W = a.W, N = a.N;
   const int ls = a.ls_col;
@@ -302,7 +302,7 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
   return r;
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 2) k_col_inv(IterArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, 3) k_col_inv(IterArgs a) {
   extern __shared__ cplx smem[];
   const int H = a.H, W = a.W;
   const int ls = a.ls_col;
@@ -336,12 +336,15 @@ static cudaError_t set_col_fwd_smem(int bytes) {
   return cudaFuncSetAttribute(k_col_fwd<FS, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+// The attribute is per kernel and process-wide, shared by every plan: it is raised to the
+// layout chooser's bound once (a launch's occupancy follows its own dynamic size).
 cudaError_t set_fused_smem_limits(const FusedGeom& g) {
+  if (g.sm_col > (size_t)kMaxDynSmem || g.sm_row > (size_t)kMaxDynSmem) return cudaErrorInvalidValue;
   cudaError_t e;
-  if ((e = set_col_fwd_smem<false>((int)g.sm_col))) return e;
-  if ((e = set_col_fwd_smem<true>((int)g.sm_col))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_col))) return e;
-  return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.sm_row);
+  if ((e = set_col_fwd_smem<false>(kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_smem<true>(kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
 }
 
 template <bool FS>

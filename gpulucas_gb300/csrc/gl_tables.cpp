@@ -9,6 +9,8 @@
 #include "gl_tables.h"
 
 #include <cmath>
+#include <thread>
+#include <vector>
 
 namespace gl {
 namespace {
@@ -99,6 +101,24 @@ inline int64_t ceil_div_pos(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 }  // namespace
 
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& chunk) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = hw ? (int64_t)hw : 1;
+  if (nt > 64) nt = 64;
+  if (n < 4096 || nt == 1) {
+    chunk(0, n);
+    return;
+  }
+  if (nt > n / 1024) nt = n / 1024;
+  std::vector<std::thread> th;
+  th.reserve((size_t)nt);
+  for (int64_t t = 0; t < nt; ++t) {
+    const int64_t b = n * t / nt, e = n * (t + 1) / nt;
+    th.emplace_back([&chunk, b, e] { chunk(b, e); });
+  }
+  for (auto& x : th) x.join();
+}
+
 int slice_depth(int p, int N) {
   if (N <= 0) return -1;
   int ratio = p / N;
@@ -137,7 +157,9 @@ void weight_entry(int p, int N, int j, double inv_scale_den, double* A, double* 
 void weight_tables(int p, int N, double inv_scale_den, std::vector<double>& A, std::vector<double>& Ainv) {
   A.resize(N);
   Ainv.resize(N);
-  for (int j = 0; j < N; ++j) weight_entry(p, N, j, inv_scale_den, &A[j], &Ainv[j]);
+  parallel_for(N, [&](int64_t b, int64_t e) {
+    for (int64_t j = b; j < e; ++j) weight_entry(p, N, (int)j, inv_scale_den, &A[j], &Ainv[j]);
+  });
 }
 
 namespace {
@@ -180,7 +202,9 @@ HostCplx pair_coeff(int64_t k, int64_t M) {
 
 void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
   tw.resize(L);
-  for (int64_t t = 0; t < L; ++t) tw[t] = twiddle(t, L);
+  parallel_for(L, [&](int64_t b, int64_t e) {
+    for (int64_t t = b; t < e; ++t) tw[t] = twiddle(t, L);
+  });
 }
 
 int stage_values(int R) {

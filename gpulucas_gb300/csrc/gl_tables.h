@@ -5,7 +5,12 @@
 #include <cstdint>
 #include <vector>
 
+#include <functional>
+
 namespace gl {
+
+// Run body(i) for i in [0, n) on the host's cores (std::thread, static chunks).
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& chunk);
 
 struct HostCplx {
   double re, im;

@@ -50,8 +50,9 @@ typedef struct {
     int check_every;       /* read the round-off status every K iterations (default 1000) */
     int use_graphs;        /* capture iteration batches in CUDA graphs (default 1) */
     int fft_h;             /* 0 = automatic; else force the column length H of M = W*H */
-    int cols_per_cta;      /* 0 = automatic; else columns per CTA in the column passes */
-    int reserved[8];
+    int cols_per_cta;      /* 0 or 1 (the column passes take one column per CTA) */
+    int autotune;          /* 1 (default): time the best few layouts once per N per process */
+    int reserved[7];
 } gl_plan_opts;
 
 typedef struct {
@@ -90,8 +91,15 @@ int gl_default_opts(gl_plan_opts* opts);
 
 /* Replaces initConstantSymbols + setSliceAndDice + mallocArrays + computeBitsPerWord(Vectors)
  * + computeWeightVectors + cufftPlan1d (gpuLucas.cu:222-237, 323-343, 948-1029, 673-714).
- * N == 0 picks N with the autotuner (findSignalSize, gpuLucas.cu:1064-1187). */
+ * N == 0 picks N with gl_find_signal_size. */
 int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** plan);
+/* findSignalSize (gpuLucas.cu:1064-1187): FFT length for exponent p.  Candidates are the
+ * even N with N/2 = 2^a 3^b 5^c 7^d (b <= 5, c <= 3, d <= 2) from the smallest the carry
+ * table accepts (p/N < 22) upward; each gets a 100-iteration round-off trial of the real
+ * test and is accepted below 0.30 (ERROR_LIMIT, gpuLucas.cu:176); among the accepted ones
+ * within 15 % of the smallest, the fastest autotuned iteration wins.  *ms_per_iter and
+ * *max_roundoff (either may be NULL) describe the choice. */
+int gl_find_signal_size(int p, const gl_plan_opts* opts, int* N_out, double* ms_per_iter, double* max_roundoff);
 /* Replaces freeArrays (gpuLucas.cu:1031-1057). */
 int gl_plan_destroy(gl_plan* plan);
 int gl_plan_get_info(const gl_plan* plan, gl_plan_info* info);

@@ -64,13 +64,13 @@ def test_describe_layouts(gl, p, N, mode):
         rh = [r for r in info.radix_h if r]
         prod = lambda xs: eval("*".join(map(str, xs))) if xs else 1  # noqa: E731
         assert prod(rw) == info.fft_w and prod(rh) == info.fft_h
-        assert set(rw + rh) <= {2, 3, 4, 5, 7, 8, 16}
+        assert set(rw + rh) <= {2, 3, 4, 5, 7, 8}
         assert info.cols_per_cta == 1
         ls = lambda L: L + L // 16 + 1  # noqa: E731  padded line stride
         assert info.smem_col == 2 * ls(info.fft_h) * 16 <= 110 * 1024
         assert info.smem_row == 4 * ls(info.fft_w) * 16 <= 110 * 1024
         assert 64 <= info.threads_col <= 256 and info.threads_col % 32 == 0
-        assert 64 <= info.threads_row <= 128 and info.threads_row % 32 == 0
+        assert 64 <= info.threads_row <= 256 and info.threads_row % 32 == 0
 
 
 def test_plan_without_gpu_reports_status(gl):

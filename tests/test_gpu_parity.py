@@ -108,3 +108,24 @@ def test_roundoff_abort_is_reported(gl):
         rep = pl.iterate(2000, check=False)
         assert rep.status == gl.GL_ERR_ROUNDOFF
         assert rep.iterations < 2000
+
+
+def test_plans_with_different_layouts_coexist(gl):
+    """Two live plans of different layouts (autotuned and forced) interleave correctly."""
+    p, N = 2976221, 163840
+    with gl.Plan(p, N) as a, gl.Plan(p, N, fft_h=640, autotune=0) as b:
+        for _ in range(3):
+            a.iterate(50)
+            b.iterate(50)
+        assert (a.products() == b.products()).all()
+
+
+def test_find_signal_size(gl, orc):
+    """findSignalSize: a usable N for p, round-off of the trial below 0.30."""
+    p = 1000003
+    N, ms, err = gl.find_signal_size(p)
+    assert N % 2 == 0 and p // N <= 21 and err < 0.30 and ms > 0
+    with gl.Plan(p, 0) as pl:
+        assert pl.info.N == N
+        pl.iterate(300)
+        assert pl.res64() == orc.Exact(p).iterate(300).res64()
