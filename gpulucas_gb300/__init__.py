@@ -103,6 +103,10 @@ def _load():
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "gl_checkpoint_write": (ctypes.c_int, [P, ctypes.c_char_p]),
+        "gl_checkpoint_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int64), vp]),
+        "gl_plan_resume": (ctypes.c_int, [P, ctypes.c_char_p]),
         "gl_iterate_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int64,
                                               ctypes.POINTER(ctypes.c_double), vp]),
     }
@@ -123,7 +127,8 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_get_products",
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
-    "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size",
+    "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
+    "gl_checkpoint_read", "gl_plan_resume",
 ]))
 
 
@@ -257,6 +262,14 @@ class Plan:
     def res64(self) -> int:
         return self.residue()[1]
 
+    def checkpoint_write(self, path: str):
+        """Write the state in the reference's <p>.chk format (old file kept as path.bak)."""
+        _check(lib.gl_checkpoint_write(self._h, os.fsencode(path)), f"checkpoint_write {path}")
+
+    def resume(self, path: str):
+        """Continue from a checkpoint in the reference's format (same p and N)."""
+        _check(lib.gl_plan_resume(self._h, os.fsencode(path)), f"resume {path}")
+
     def mersenne_test(self, iters: int = 0) -> Result:
         res = Result()
         st = lib.gl_mersenne_test(self._h, int(iters), ctypes.byref(res))
@@ -286,6 +299,20 @@ def error_test(p: int, N: int, iters: int = 0, **opts) -> IterReport:
     o = default_opts(**opts)
     _check(lib.gl_error_test(int(p), int(N), ctypes.byref(o), int(iters), ctypes.byref(rep)), "error_test")
     return rep
+
+
+def checkpoint_read(path: str, p: int, with_digits: bool = True):
+    """(N, squarings done, digits or None) of a checkpoint in the reference's format."""
+    N = ctypes.c_int()
+    k = ctypes.c_int64()
+    _check(lib.gl_checkpoint_read(os.fsencode(path), int(p), ctypes.byref(N), ctypes.byref(k), None),
+           f"checkpoint_read {path}")
+    digits = None
+    if with_digits:
+        digits = np.empty(N.value, np.int32)
+        _check(lib.gl_checkpoint_read(os.fsencode(path), int(p), ctypes.byref(N), ctypes.byref(k),
+                                      _ptr(digits)), f"checkpoint_read {path}")
+    return N.value, k.value, digits
 
 
 def find_signal_size(p: int, **opts):

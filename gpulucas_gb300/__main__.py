@@ -2,20 +2,32 @@
 
     python -m gpulucas_gb300 [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] [p]
 
--f N    FFT length (the reference requires N % 256 == 0; here N must be even with
-        N/2 = 2^a 3^b 5^c 7^d)
+-f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); without -f the length is chosen as
+        findSignalSize does (gpuLucas.cu:1064-1187)
 -n p    exponent (or give p as the positional argument)
 -d dev  CUDA device
--c freq round-off status check interval in iterations
+-c freq checkpoint every freq iterations to <p>.chk in the reference's format
+        (gpuLucas.cu:1414-1423); a run finding <p>.chk or <p>.chk.bak resumes from it
 -k k    stop after k iterations and print Res64 (0 = full p-2 test)
 -m      execution form: fused (default) or plain
-A full test appends the reference's result line to results.txt (gpuLucas.cu:1514-1548).
+SIGINT / SIGTERM write a checkpoint and exit (gpuLucas.cu:365-369, 1425-1429).
+A full test appends the reference's result line to results.txt (gpuLucas.cu:1514-1548)
+and removes its checkpoint files (gpuLucas.cu:628-632).
 """
 from __future__ import annotations
 
 import argparse
+import os
+import signal
 import sys
 import time
+
+_stop = False
+
+
+def _on_signal(sig, frame):
+    global _stop
+    _stop = True
 
 
 def main(argv=None) -> int:
@@ -26,7 +38,7 @@ def main(argv=None) -> int:
     ap.add_argument("-f", type=int, default=0)
     ap.add_argument("-n", type=int, default=0)
     ap.add_argument("-d", type=int, default=0)
-    ap.add_argument("-c", type=int, default=1000)
+    ap.add_argument("-c", type=int, default=0)
     ap.add_argument("-k", type=int, default=0)
     ap.add_argument("-m", choices=["fused", "plain"], default="fused")
     ap.add_argument("p", nargs="?", type=int, default=0)
@@ -38,30 +50,75 @@ def main(argv=None) -> int:
     if not p:
         print("testPrime not specified, aborting", file=sys.stderr)
         return 2
-    if not a.f:
-        print("an FFT length -f N is required", file=sys.stderr)
-        return 2
     import gpulucas_gb300 as gl
     mode = gl.MODE_FUSED if a.m == "fused" else gl.MODE_PLAIN
-    t0 = time.time()
-    with gl.Plan(p, a.f, mode=mode, device=a.d, check_every=max(1, a.c)) as pl:
+    chk = f"{p}.chk"
+    resume_k = None
+    N = a.f
+    if os.path.exists(chk) or os.path.exists(chk + ".bak"):
+        try:
+            Nc, resume_k, _ = gl.checkpoint_read(chk, p, with_digits=False)
+            if N and N != Nc:
+                print(f"checkpoint {chk} has N = {Nc}, not {N}; not resuming", file=sys.stderr)
+                resume_k = None
+            else:
+                N = Nc
+        except gl.GLError as e:
+            print(f"ignoring checkpoint: {e}", file=sys.stderr)
+            resume_k = None
+    if not N:
+        N, ms, err = gl.find_signal_size(p, device=a.d)
         if not a.q:
-            i = pl.info
-            print(f"Testing M{p}, word sizes ({i.lo_bits}, {i.hi_bits}), FFT length {a.f} "
+            print(f"Optimal signalSize detected: {N} ({ms:.4f} ms/iter, trial round-off {err:.4f})")
+    total = a.k if a.k else p - 2
+    signal.signal(signal.SIGINT, _on_signal)
+    signal.signal(signal.SIGTERM, _on_signal)
+    t0 = time.time()
+    with gl.Plan(p, N, mode=mode, device=a.d) as pl:
+        i = pl.info
+        if resume_k is not None:
+            pl.resume(chk)
+            done = resume_k
+            if not a.q:
+                print(f"Resuming M{p} at iteration {done} from {chk}")
+        else:
+            pl.reset()
+            done = 0
+        if not a.q:
+            print(f"Testing M{p}, word sizes ({i.lo_bits}, {i.hi_bits}), FFT length {N} "
                   f"({i.fft_h} x {i.fft_w} complex), carry depth {i.carry_depth}, form {a.m}")
-        res = pl.mersenne_test(a.k)
+        step = a.c if a.c > 0 else max(1, total - done)
+        ms_total, maxerr = 0.0, 0.0
+        while done < total and not _stop:
+            n = min(step, total - done)
+            rep = pl.iterate(n)
+            done += n
+            ms_total += rep.ms
+            maxerr = max(maxerr, rep.max_roundoff)
+            if a.c > 0 and (done < total or _stop):
+                pl.checkpoint_write(chk)
+                if a.v:
+                    print(f"[{100.0 * done / total:4.1f}%] Iter {done}: {rep.ms / n:.4f} ms/iter, "
+                          f"0x{pl.res64():016x}")
+        if _stop and done < total:
+            pl.checkpoint_write(chk)
+            print(f"Interrupted at iteration {done}; checkpoint written to {chk}")
+            return 130
+        _, r, z = pl.residue()
     dt = time.time() - t0
     if a.k:
-        print(f"M( {p} ) Iter {res.iterations}: 0x{res.res64:016x}, max round-off {res.max_roundoff:.4f}, "
-              f"{res.ms / max(1, res.iterations):.4f} ms/iter, n = {a.f}")
+        print(f"M( {p} ) Iter {done}: 0x{r:016x}, max round-off {maxerr:.4f}, "
+              f"{ms_total / max(1, done - (resume_k or 0)):.4f} ms/iter, n = {N}")
         return 0
-    line = (f"M( {p} )P, n = {a.f}, gpulucas_gb300" if res.is_prime
-            else f"M( {p} )C, 0x{res.res64:016x}, n = {a.f}, gpulucas_gb300")
+    line = f"M( {p} )P, n = {N}, gpulucas_gb300" if z else f"M( {p} )C, 0x{r:016x}, n = {N}, gpulucas_gb300"
     print(line)
     if a.v:
-        print(f"max round-off {res.max_roundoff:.4f}, {dt:.1f} s")
+        print(f"max round-off {maxerr:.4f}, {dt:.1f} s")
     with open("results.txt", "a") as f:
         f.write(line + "\n")
+    for path in (chk, chk + ".bak"):
+        if os.path.exists(path):
+            os.remove(path)
     return 0
 
 

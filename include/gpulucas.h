@@ -141,6 +141,23 @@ int gl_set_carry_state(gl_plan* plan, const int32_t* digit, const int8_t* hi, in
  * (may be NULL), Res64 and the exact zero test of the current state. */
 int gl_get_residue(gl_plan* plan, int32_t* digits_out, uint64_t* res64, int* is_zero);
 
+/* --- checkpoints in the reference's file format --------------------------- */
+
+/* writeCheckpoint (gpuLucas.cu:1641-1665): char[16] "gpuLucas", char[16] "0.9.4", int p,
+ * int N, int iter, then N doubles of the weighted FFT input A[j](digit[j] + hi[j-1])
+ * (d_signal).  iter follows the reference's loop count: a state after k squarings is
+ * written with iter = k + 1.  The old file is kept as path.bak; the new one is written
+ * to a temporary name and renamed, so a crash never leaves a torn checkpoint. */
+int gl_checkpoint_write(gl_plan* plan, const char* path);
+/* readCheckpoint (gpuLucas.cu:1569-1639): header checks (name "gpuLucas", p), N, the
+ * squarings done (iter - 1) and, if digits_out is not NULL (N int32), the digit vector
+ * round(d[j] / A[j]).  Falls back to path.bak when path is missing or unreadable.
+ * GL_ERR_IO / GL_ERR_CHECKPOINT on failure; needs no GPU. */
+int gl_checkpoint_read(const char* path, int p, int* N_out, int64_t* iterations_out, int32_t* digits_out);
+/* Resume a plan (same p and N) from a checkpoint: the next iteration's FFT input equals
+ * the saved d_signal bit for bit, as the reference's resume (gpuLucas.cu:1361-1363). */
+int gl_plan_resume(gl_plan* plan, const char* path);
+
 /* --- reference entry points (README: errorTest / mersenneTest) ---------- */
 
 /* errorTrial (gpuLucas.cu:1192-1282) as README's errorTest(p, N): runs
