@@ -53,6 +53,12 @@ class PlanInfo(ctypes.Structure):
                 ("smem_col", ctypes.c_int), ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("ntests", ctypes.c_int), ("col_units", ctypes.c_int), ("row_units", ctypes.c_int),
+                ("threads_col", ctypes.c_int), ("threads_row", ctypes.c_int), ("smem_col", ctypes.c_int),
+                ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t), ("iterations", ctypes.c_int64)]
+
+
 class IterReport(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("total_iterations", ctypes.c_int64),
                 ("max_roundoff", ctypes.c_double), ("ms", ctypes.c_double), ("status", ctypes.c_int)]
@@ -103,6 +109,16 @@ def _load():
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "gl_smallest_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
+        "gl_batch_create": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
+        "gl_batch_destroy": (ctypes.c_int, [P]),
+        "gl_batch_iterate": (ctypes.c_int, [P, ctypes.c_int64, ctypes.POINTER(IterReport)]),
+        "gl_batch_stream": (ctypes.c_int, [P, PP]),
+        "gl_batch_enqueue": (ctypes.c_int, [P, ctypes.c_int64]),
+        "gl_batch_sync_status": (ctypes.c_int, [P, ctypes.POINTER(IterReport)]),
+        "gl_batch_result": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(Result), ctypes.POINTER(ctypes.c_int)]),
+        "gl_batch_get_info": (ctypes.c_int, [P, ctypes.POINTER(BatchInfo)]),
+        "gl_batch_test_info": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(PlanInfo)]),
         "gl_checkpoint_write": (ctypes.c_int, [P, ctypes.c_char_p]),
         "gl_checkpoint_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                               ctypes.POINTER(ctypes.c_int64), vp]),
@@ -128,7 +144,9 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
     "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
-    "gl_checkpoint_read", "gl_plan_resume",
+    "gl_checkpoint_read", "gl_plan_resume", "gl_smallest_signal_size", "gl_batch_create", "gl_batch_destroy",
+    "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
+    "gl_batch_get_info", "gl_batch_test_info",
 ]))
 
 
@@ -275,6 +293,81 @@ class Plan:
         st = lib.gl_mersenne_test(self._h, int(iters), ctypes.byref(res))
         _check(st, "mersenne_test")
         return res
+
+
+class Batch:
+    """Many LL tests advanced together by one set of launches per iteration."""
+
+    def __init__(self, ps, Ns=None, **opts):
+        ps = np.ascontiguousarray(ps, np.int32)
+        Ns = np.zeros_like(ps) if Ns is None else np.ascontiguousarray(Ns, np.int32)
+        assert ps.shape == Ns.shape and ps.ndim == 1 and ps.size > 0
+        o = default_opts(**opts)
+        h = ctypes.c_void_p()
+        _check(lib.gl_batch_create(_ptr(ps), _ptr(Ns), int(ps.size), ctypes.byref(o), ctypes.byref(h)),
+               f"batch of {ps.size}")
+        self._h = h
+        self.ntests = int(ps.size)
+        self.info = BatchInfo()
+        _check(lib.gl_batch_get_info(self._h, ctypes.byref(self.info)), "batch info")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.gl_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, iters: int, check: bool = True) -> IterReport:
+        rep = IterReport()
+        st = lib.gl_batch_iterate(self._h, int(iters), ctypes.byref(rep))
+        if check:
+            _check(st, "batch iterate")
+        return rep
+
+    def enqueue(self, iters: int):
+        _check(lib.gl_batch_enqueue(self._h, int(iters)), "batch enqueue")
+
+    def sync_status(self, check: bool = True) -> IterReport:
+        rep = IterReport()
+        st = lib.gl_batch_sync_status(self._h, ctypes.byref(rep))
+        if check:
+            _check(st, "batch status")
+        return rep
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _check(lib.gl_batch_stream(self._h, ctypes.byref(s)), "batch stream")
+        return s.value or 0
+
+    def test_info(self, i: int) -> PlanInfo:
+        info = PlanInfo()
+        _check(lib.gl_batch_test_info(self._h, int(i), ctypes.byref(info)), "batch test info")
+        return info
+
+    def result(self, i: int):
+        """(Result, status) of test i."""
+        r = Result()
+        st = ctypes.c_int()
+        _check(lib.gl_batch_result(self._h, int(i), ctypes.byref(r), ctypes.byref(st)), f"batch result {i}")
+        return r, st.value
+
+
+def smallest_signal_size(p: int, max_bits_per_word: float = 19.5) -> int:
+    N = ctypes.c_int()
+    _check(lib.gl_smallest_signal_size(int(p), float(max_bits_per_word), ctypes.byref(N)), "smallest_signal_size")
+    return N.value
 
 
 # reference-named entry points ---------------------------------------------------

@@ -1,0 +1,335 @@
+// gl_batch.cpp -- many Lucas-Lehmer tests advanced together.
+//
+// Each test keeps a fused-form plan (its own tables and buffers, layout chosen for
+// total work since the batch, not the test, fills the device).  The batch uploads a
+// descriptor table of every test's iteration arguments and two unit maps -- one entry
+// per column (column passes) and per row pair (row pass), ordered longest unit first
+// -- so one set of three launches advances every test by one iteration.  Batches of
+// 64 iterations are replayed from one CUDA graph.  Each test's round-off status word
+// lives in one contiguous array read back with a single copy.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gl_internal.h"
+#include "gl_plan.h"
+#include "gl_tables.h"
+
+using namespace gl;
+
+struct gl_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<gl_plan*> plans;
+  std::vector<void*> allocs;
+  BatchLaunch launch{};
+  Status* d_status = nullptr;
+  std::vector<Status> h_status;
+  std::vector<double> maxerr;  // per test, over the run
+  int64_t iters_done = 0;
+  int check_every = 1000;
+  double error_limit = 0.4;
+  cudaGraphExec_t gexec = nullptr;
+  size_t device_bytes = 0;
+};
+
+namespace {
+
+constexpr int kBatchGraph = 64;
+
+void free_batch(gl_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  for (gl_plan* p : b->plans) gl_plan_destroy(p);
+  delete b;
+}
+
+template <typename T>
+int upload(gl_batch* b, T** dst, const std::vector<T>& v) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(1, v.size())) != cudaSuccess) return GL_ERR_NOMEM;
+  b->allocs.push_back(p);
+  b->device_bytes += sizeof(T) * v.size();
+  if (!v.empty() && cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GL_ERR_CUDA;
+  *dst = static_cast<T*>(p);
+  return GL_OK;
+}
+
+int launch_n(gl_batch* b, int64_t k) {
+  for (int64_t i = 0; i < k; ++i)
+    if (launch_batch_iteration(b->launch, b->stream, false) != cudaSuccess) return GL_ERR_CUDA;
+  return GL_OK;
+}
+
+int enqueue(gl_batch* b, int64_t k) {
+  if (k >= kBatchGraph) {
+    if (!b->gexec) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GL_ERR_CUDA;
+      const int rc = launch_n(b, kBatchGraph);
+      const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+      if (rc != GL_OK || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return GL_ERR_CUDA;
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&b->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) {
+        b->gexec = nullptr;
+        return GL_ERR_CUDA;
+      }
+    }
+    while (k >= kBatchGraph) {
+      if (cudaGraphLaunch(b->gexec, b->stream) != cudaSuccess) return GL_ERR_CUDA;
+      k -= kBatchGraph;
+    }
+  }
+  return launch_n(b, k);
+}
+
+// Reads every test's status; returns the worst status and the max round-off.
+int read_status(gl_batch* b, double* worst_err) {
+  const size_t n = b->plans.size();
+  if (cudaMemcpyAsync(b->h_status.data(), b->d_status, sizeof(Status) * n, cudaMemcpyDeviceToHost, b->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return GL_ERR_CUDA;
+  int st = GL_OK;
+  double worst = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    const double e = std::ldexp((double)b->h_status[i].maxerr64, -64);
+    b->maxerr[i] = std::max(b->maxerr[i], e);
+    worst = std::max(worst, e);
+    if (b->h_status[i].flags) st = GL_ERR_OVERFLOW;
+    else if (e >= b->error_limit && st == GL_OK) st = GL_ERR_ROUNDOFF;
+  }
+  if (worst_err) *worst_err = worst;
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out) {
+  if (!N_out || p < 64 || !(max_bits_per_word > 1.0)) return GL_ERR_ARG;
+  const int64_t cap = 1 << 27;
+  int best = 0;
+  for (int64_t p2 = 2; p2 <= cap; p2 *= 2)
+    for (int64_t p3 = p2; p3 <= cap; p3 *= 3)
+      for (int64_t p5 = p3; p5 <= cap; p5 *= 5)
+        for (int64_t N = p5; N <= cap; N *= 7) {
+          if (N < 64 || (double)p / (double)N > max_bits_per_word) continue;
+          if (slice_depth(p, (int)N) < 0) continue;
+          if (!best || N < best) best = (int)N;
+        }
+  if (!best) return GL_ERR_SIZE;
+  *N_out = best;
+  return GL_OK;
+}
+
+int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* opts, gl_batch** out) {
+  if (!p || !out || ntests < 1) return GL_ERR_ARG;
+  *out = nullptr;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  o.mode = GL_MODE_FUSED;
+  o.autotune = 0;
+  o.fft_h = 0;
+  gl_batch* b = new gl_batch();
+  b->device = o.device;
+  b->check_every = o.check_every;
+  b->error_limit = o.error_limit;
+#define GB_TRY(x)      \
+  do {                 \
+    int r_ = (x);      \
+    if (r_ != GL_OK) { \
+      free_batch(b);   \
+      return r_;       \
+    }                  \
+  } while (0)
+  if (cudaSetDevice(o.device) != cudaSuccess) {
+    delete b;
+    return GL_ERR_NODEVICE;
+  }
+  GB_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess ? GL_OK : GL_ERR_CUDA);
+  for (int i = 0; i < ntests; ++i) {
+    int n_i = N ? N[i] : 0;
+    if (n_i == 0) GB_TRY(gl_smallest_signal_size(p[i], 19.5, &n_i));
+    gl_plan* pl = nullptr;
+    GB_TRY(gl_plan_create_ex(p[i], n_i, &o, 1, &pl));
+    b->plans.push_back(pl);
+    b->device_bytes += pl->device_bytes;
+  }
+  // per-test status words, one contiguous array
+  std::vector<Status> zero((size_t)ntests);
+  std::memset(zero.data(), 0, sizeof(Status) * zero.size());
+  GB_TRY(upload(b, &b->d_status, zero));
+  b->h_status.resize((size_t)ntests);
+  b->maxerr.assign((size_t)ntests, 0.0);
+  std::vector<IterArgs> desc((size_t)ntests);
+  int t_col = 64, t_row = 64;
+  size_t sm_col = 0, sm_row = 0;
+  for (int i = 0; i < ntests; ++i) {
+    desc[i] = b->plans[i]->args;
+    desc[i].status = b->d_status + i;
+    t_col = std::max(t_col, b->plans[i]->fg.t_col);
+    t_row = std::max(t_row, b->plans[i]->fg.t_row);
+    sm_col = std::max(sm_col, b->plans[i]->fg.sm_col);
+    sm_row = std::max(sm_row, b->plans[i]->fg.sm_row);
+  }
+  IterArgs* d_desc = nullptr;
+  GB_TRY(upload(b, &d_desc, desc));
+  // unit maps, longest units first so the tail of each launch is short work
+  std::vector<int> order((size_t)ntests);
+  for (int i = 0; i < ntests; ++i) order[i] = i;
+  std::vector<int2> cols, rows;
+  std::sort(order.begin(), order.end(), [&](int a, int c) {
+    return gl_plan_unit_cost(b->plans[a], false) > gl_plan_unit_cost(b->plans[c], false);
+  });
+  for (int t : order)
+    for (int u = 0; u < b->plans[t]->fg.W; ++u) cols.push_back(make_int2(t, u));
+  std::sort(order.begin(), order.end(), [&](int a, int c) {
+    return gl_plan_unit_cost(b->plans[a], true) > gl_plan_unit_cost(b->plans[c], true);
+  });
+  for (int t : order)
+    for (int u = 0; u <= b->plans[t]->fg.H / 2; ++u) rows.push_back(make_int2(t, u));
+  int2 *d_cols = nullptr, *d_rows = nullptr;
+  GB_TRY(upload(b, &d_cols, cols));
+  GB_TRY(upload(b, &d_rows, rows));
+  b->launch.tests = d_desc;
+  b->launch.col_units = d_cols;
+  b->launch.row_units = d_rows;
+  b->launch.ncol = (int)cols.size();
+  b->launch.nrow = (int)rows.size();
+  b->launch.t_col = t_col;
+  b->launch.t_row = t_row;
+  b->launch.sm_col = sm_col;
+  b->launch.sm_row = sm_row;
+  GB_TRY(set_batch_smem_limits() == cudaSuccess ? GL_OK : GL_ERR_CUDA);
+  GB_TRY(cudaDeviceSynchronize() == cudaSuccess ? GL_OK : GL_ERR_CUDA);
+#undef GB_TRY
+  *out = b;
+  return GL_OK;
+}
+
+int gl_batch_destroy(gl_batch* b) {
+  if (!b) return GL_ERR_ARG;
+  free_batch(b);
+  return GL_OK;
+}
+
+int gl_batch_stream(gl_batch* b, void** stream) {
+  if (!b || !stream) return GL_ERR_ARG;
+  *stream = (void*)b->stream;
+  return GL_OK;
+}
+
+int gl_batch_enqueue(gl_batch* b, int64_t iters) {
+  if (!b || iters < 0) return GL_ERR_ARG;
+  if (cudaSetDevice(b->device) != cudaSuccess) return GL_ERR_CUDA;
+  const int rc = enqueue(b, iters);
+  if (rc != GL_OK) return rc;
+  b->iters_done += iters;
+  for (gl_plan* p : b->plans) gl_plan_note_external_iterations(p, iters);
+  return GL_OK;
+}
+
+int gl_batch_iterate(gl_batch* b, int64_t iters, gl_iter_report* rep) {
+  if (!b || iters < 0) return GL_ERR_ARG;
+  if (cudaSetDevice(b->device) != cudaSuccess) return GL_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return GL_ERR_CUDA;
+  cudaEventRecord(e0, b->stream);
+  int64_t done = 0;
+  int st = GL_OK;
+  double worst = 0.0;
+  while (done < iters) {
+    const int64_t k = std::min<int64_t>(iters - done, b->check_every);
+    st = gl_batch_enqueue(b, k);
+    if (st != GL_OK) break;
+    done += k;
+    double e = 0.0;
+    st = read_status(b, &e);
+    worst = std::max(worst, e);
+    if (st != GL_OK) break;
+  }
+  cudaEventRecord(e1, b->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rep) {
+    rep->iterations = done;
+    rep->total_iterations = b->iters_done;
+    rep->max_roundoff = worst;
+    rep->ms = ms;
+    rep->status = st;
+  }
+  return st;
+}
+
+int gl_batch_sync_status(gl_batch* b, gl_iter_report* rep) {
+  if (!b) return GL_ERR_ARG;
+  double e = 0.0;
+  const int st = read_status(b, &e);
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    rep->total_iterations = b->iters_done;
+    rep->max_roundoff = e;
+    rep->status = st;
+  }
+  return st;
+}
+
+int gl_batch_result(gl_batch* b, int index, gl_result* r, int* status) {
+  if (!b || !r || index < 0 || index >= (int)b->plans.size()) return GL_ERR_ARG;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return GL_ERR_CUDA;
+  gl_plan* pl = b->plans[(size_t)index];
+  uint64_t res = 0;
+  int z = 0;
+  const int rc = gl_get_residue(pl, nullptr, &res, &z);
+  if (rc != GL_OK) return rc;
+  std::memset(r, 0, sizeof(*r));
+  r->p = pl->p;
+  r->N = pl->N;
+  r->iterations = pl->iters_done;
+  r->is_zero = z;
+  r->is_prime = (pl->iters_done == (int64_t)pl->p - 2 && z) ? 1 : 0;
+  r->res64 = res;
+  r->max_roundoff = b->maxerr[(size_t)index];
+  if (status) {
+    const Status& s = b->h_status[(size_t)index];
+    *status = s.flags ? GL_ERR_OVERFLOW : (b->maxerr[(size_t)index] >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK);
+  }
+  return GL_OK;
+}
+
+int gl_batch_get_info(const gl_batch* b, gl_batch_info* info) {
+  if (!b || !info) return GL_ERR_ARG;
+  std::memset(info, 0, sizeof(*info));
+  info->ntests = (int)b->plans.size();
+  info->col_units = b->launch.ncol;
+  info->row_units = b->launch.nrow;
+  info->threads_col = b->launch.t_col;
+  info->threads_row = b->launch.t_row;
+  info->smem_col = (int)b->launch.sm_col;
+  info->smem_row = (int)b->launch.sm_row;
+  info->device_bytes = b->device_bytes;
+  info->iterations = b->iters_done;
+  return GL_OK;
+}
+
+int gl_batch_test_info(const gl_batch* b, int index, gl_plan_info* info) {
+  if (!b || index < 0 || index >= (int)b->plans.size()) return GL_ERR_ARG;
+  return gl_plan_get_info(b->plans[(size_t)index], info);
+}
+
+}  // extern "C"

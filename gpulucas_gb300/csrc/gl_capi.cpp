@@ -11,31 +11,10 @@
 #include <vector>
 
 #include "gl_internal.h"
+#include "gl_plan.h"
 #include "gl_tables.h"
 
 using namespace gl;
-
-struct gl_plan {
-  int p = 0, N = 0, M = 0, LO = 0, n = 0;
-  int mode = GL_MODE_FUSED, device = 0;
-  double error_limit = 0.4;
-  int check_every = 1000;
-  int use_graphs = 1;
-  cudaStream_t stream = nullptr;
-  FusedGeom fg{};
-  PlainGeom pg{};
-  IterArgs args{};
-  std::vector<void*> allocs;
-  Status* h_status = nullptr;  // pinned
-  int64_t iters_done = 0;
-  double run_maxerr = 0.0;
-  bool from_state = false;     // next fused iteration loads (digit, hi)
-  bool carry_valid = true;     // device (digit, hi) matches the current products
-  cudaGraphExec_t gexec = nullptr;
-  int gexec_iters = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  size_t device_bytes = 0;
-};
 
 namespace {
 
@@ -423,6 +402,23 @@ int setSliceAndDice(int testPrime, int signalSize) {
 }
 
 int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
+  return gl_plan_create_ex(p, N, opts, 0, out);
+}
+
+}  // extern "C"
+
+void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters) {
+  pl->iters_done += iters;
+  pl->from_state = false;
+  pl->carry_valid = pl->mode == GL_MODE_PLAIN;
+}
+
+double gl_plan_unit_cost(const gl_plan* pl, bool row) {
+  if (row) return 2.0 * pl->fg.W * (2.0 * line_ops(pl->fg.pw) + 16.0);
+  return pl->fg.H * (line_ops(pl->fg.ph) + 6.0);
+}
+
+int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, gl_plan** out) {
   if (!out) return GL_ERR_ARG;
   *out = nullptr;
   gl_plan_opts o;
@@ -447,8 +443,10 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
   if (cudaSetDevice(o.device) != cudaSuccess) return GL_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess) return GL_ERR_CUDA;
+  if (sms_override > 0) sms = sms_override;
   int force_h = o.fft_h;
-  if (o.mode == GL_MODE_FUSED && !force_h && o.autotune) force_h = autotune_layout(M, n, sms, 0, nullptr);
+  if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override)
+    force_h = autotune_layout(M, n, sms, 0, nullptr);
   int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg) : choose_plain_geom(M, &pg);
   if (rc != GL_OK) return rc;
 
@@ -576,6 +574,8 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
 #undef GL_TRY
 #undef GL_TRYC
 }
+
+extern "C" {
 
 int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info) {
   if (!info) return GL_ERR_ARG;

@@ -81,6 +81,17 @@ struct IterArgs {
   LinePlan pw, ph;
 };
 
+// A batch of fused-form tests advanced by one set of launches: the descriptor table of
+// every test's arguments (device) and the unit maps (test, local column / row pair).
+struct BatchLaunch {
+  const IterArgs* tests;
+  const int2* col_units;
+  const int2* row_units;
+  int ncol, nrow;
+  int t_col, t_row;
+  size_t sm_col, sm_row;
+};
+
 // launchers (gl_kernels.cu); all asynchronous on `s`
 // from_state: the first column pass loads the carry-save state (digit, hi) instead of
 // dicing the products, exactly as loadIntToDoubleIBDWT (gpuLucas.cu:730-766) does
@@ -97,6 +108,8 @@ cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
 cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
                                  cudaStream_t s);
 cudaError_t set_fused_smem_limits(const FusedGeom& g);
+cudaError_t set_batch_smem_limits();
+cudaError_t launch_batch_iteration(const BatchLaunch& b, cudaStream_t s, bool from_state);
 cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s);
 
 }  // namespace gl

@@ -146,11 +146,10 @@ __device__ __forceinline__ int colmajor(const IterArgs& a, int j) {
 // j0 = 2m, j0+1 the digit sums of j0-1, j0, j0+1 need the products of words
 // j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.
 template <bool FROM_STATE, int NC>
-__global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
+__device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
   extern __shared__ cplx smem[];
   const int H = a.H, W = a.W, N = a.N;
   const int ls = a.ls_col;
-  const int m1 = blockIdx.x;
   cplx* buf1 = smem + ls;
   for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
     const int j0 = 2 * (m1 + W * m2);
@@ -210,11 +209,15 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
     st(a.Z + (size_t)k2 * W + m1, cmul(res[pad(k2)], ld(tw + k2)));
 }
 
-__global__ void __launch_bounds__(kRowThreads, 3) k_row_sq(IterArgs a) {
+template <bool FROM_STATE, int NC>
+__global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
+  col_fwd_body<FROM_STATE, NC>(a, blockIdx.x);
+}
+
+__device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 .. H/2 */) {
   extern __shared__ cplx smem[];
   const int W = a.W, H = a.H;
   const int ls = a.ls_row;
-  const int c = blockIdx.x;  // 0 .. H/2
   const int ra = c, rb = H - c;
   const bool self = (c == 0) || (2 * c == H);
   const int nl = self ? 1 : 2;
@@ -265,6 +268,8 @@ __global__ void __launch_bounds__(kRowThreads, 3) k_row_sq(IterArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(kRowThreads, 3) k_row_sq(IterArgs a) { row_sq_body(a, blockIdx.x); }
+
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -302,11 +307,10 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
   return r;
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 3) k_col_inv(IterArgs a) {
+__device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   extern __shared__ cplx smem[];
   const int H = a.H, W = a.W;
   const int ls = a.ls_col;
-  const int m1 = blockIdx.x;
   cplx* buf1 = smem + ls;
   for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z + (size_t)k2 * W + m1);
   __syncthreads();
@@ -324,6 +328,69 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_col_inv(IterArgs a) {
     *reinterpret_cast<longlong2*>(a.ll + s0) = make_longlong2(r0, r1);
   }
   finish_status(a, emax, fl);
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 3) k_col_inv(IterArgs a) { col_inv_body(a, blockIdx.x); }
+
+// ---------------------------------------------------------------------------
+// Batched kernels: many tests advance together.  units[blockIdx.x] = (test, local
+// unit); each test's arguments come from the descriptor table.  Dynamic shared memory
+// and block size are the maxima over the batch; the line FFTs loop over butterflies,
+// so a smaller test simply leaves threads idle in some stages.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load_desc(const IterArgs* __restrict__ tests, int t, IterArgs& sa) {
+  // IterArgs is a plain struct of ints and pointers: copy it word by word
+  const int* src = reinterpret_cast<const int*>(tests + t);
+  int* dst = reinterpret_cast<int*>(&sa);
+  for (int i = threadIdx.x; i < (int)(sizeof(IterArgs) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+}
+
+template <bool FROM_STATE>
+__global__ void __launch_bounds__(kMaxThreads, 2) kb_col_fwd(const IterArgs* __restrict__ tests,
+                                                             const int2* __restrict__ units) {
+  __shared__ IterArgs sa;
+  const int2 u = units[blockIdx.x];
+  load_desc(tests, u.x, sa);
+  switch (sa.n) {
+    case 2: col_fwd_body<FROM_STATE, 2>(sa, u.y); break;
+    case 3: col_fwd_body<FROM_STATE, 3>(sa, u.y); break;
+    case 4: col_fwd_body<FROM_STATE, 4>(sa, u.y); break;
+    case 5: col_fwd_body<FROM_STATE, 5>(sa, u.y); break;
+    default: col_fwd_body<FROM_STATE, 6>(sa, u.y); break;
+  }
+}
+
+__global__ void __launch_bounds__(kRowThreads, 3) kb_row_sq(const IterArgs* __restrict__ tests,
+                                                            const int2* __restrict__ units) {
+  __shared__ IterArgs sa;
+  const int2 u = units[blockIdx.x];
+  load_desc(tests, u.x, sa);
+  row_sq_body(sa, u.y);
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 3) kb_col_inv(const IterArgs* __restrict__ tests,
+                                                             const int2* __restrict__ units) {
+  __shared__ IterArgs sa;
+  const int2 u = units[blockIdx.x];
+  load_desc(tests, u.x, sa);
+  col_inv_body(sa, u.y);
+}
+
+cudaError_t set_batch_smem_limits() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(kb_col_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(kb_col_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(kb_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  return cudaFuncSetAttribute(kb_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+}
+
+cudaError_t launch_batch_iteration(const BatchLaunch& b, cudaStream_t s, bool from_state) {
+  if (from_state) kb_col_fwd<true><<<b.ncol, b.t_col, b.sm_col, s>>>(b.tests, b.col_units);
+  else kb_col_fwd<false><<<b.ncol, b.t_col, b.sm_col, s>>>(b.tests, b.col_units);
+  kb_row_sq<<<b.nrow, b.t_row, b.sm_row, s>>>(b.tests, b.row_units);
+  kb_col_inv<<<b.ncol, b.t_col, b.sm_col, s>>>(b.tests, b.col_units);
+  return cudaGetLastError();
 }
 
 template <bool FS>

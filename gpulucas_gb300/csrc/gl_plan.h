@@ -1,0 +1,42 @@
+// gl_plan.h -- the plan object shared by the C ABI translation units (internal).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "gl_internal.h"
+
+using gl::FusedGeom;
+using gl::IterArgs;
+using gl::PlainGeom;
+using gl::Status;
+
+struct gl_plan {
+  int p = 0, N = 0, M = 0, LO = 0, n = 0;
+  int mode = GL_MODE_FUSED, device = 0;
+  double error_limit = 0.4;
+  int check_every = 1000;
+  int use_graphs = 1;
+  cudaStream_t stream = nullptr;
+  FusedGeom fg{};
+  PlainGeom pg{};
+  IterArgs args{};
+  std::vector<void*> allocs;
+  Status* h_status = nullptr;  // pinned
+  int64_t iters_done = 0;
+  double run_maxerr = 0.0;
+  bool from_state = false;     // next fused iteration loads (digit, hi)
+  bool carry_valid = true;     // device (digit, hi) matches the current products
+  cudaGraphExec_t gexec = nullptr;
+  int gexec_iters = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  size_t device_bytes = 0;
+};
+
+
+// gl_plan_create with an explicit SM count for the layout cost model (1 = a member of
+// a batch: minimise total work, the batch spreads units over the device).
+int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, gl_plan** out);
+// iterations done outside the plan's own launches (by a batch): bookkeeping only
+void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters);
+// cost of one column-pass unit and one row-pass unit of a fused plan (FP64 model)
+double gl_plan_unit_cost(const gl_plan* pl, bool row);

@@ -175,6 +175,40 @@ int setSliceAndDice(int testPrime, int signalSize);
 int gl_error_test(int p, int N, const gl_plan_opts* opts, int iters, gl_iter_report* report);
 int gl_mersenne_test(gl_plan* plan, int64_t iters, gl_result* result);
 
+/* --- batches: many tests advanced together ------------------------------- */
+
+/* No counterpart in the reference (it runs one test per process).  Smallest even N with
+ * N/2 = 2^a 3^b 5^c 7^d (any exponents) and p/N <= max_bits_per_word (the batch
+ * configuration uses 19.5). */
+int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out);
+
+typedef struct gl_batch gl_batch;
+typedef struct {
+    int ntests;
+    int col_units, row_units;      /* CTAs per column-pass / row-pass launch */
+    int threads_col, threads_row;
+    int smem_col, smem_row;
+    size_t device_bytes;
+    int64_t iterations;            /* iterations every test has done */
+} gl_batch_info;
+
+/* One fused-form plan per test (N[i] == 0: gl_smallest_signal_size(p[i], 19.5)), a
+ * device descriptor table of their arguments, and unit maps so that three launches
+ * advance every test by one iteration (64-iteration CUDA graphs).  opts: device,
+ * error_limit, check_every. */
+int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* opts, gl_batch** batch);
+int gl_batch_destroy(gl_batch* batch);
+/* All tests advance `iters` iterations; per-test round-off is checked every check_every.
+ * Returns the worst status (GL_ERR_ROUNDOFF / GL_ERR_OVERFLOW name some test). */
+int gl_batch_iterate(gl_batch* batch, int64_t iters, gl_iter_report* report);
+int gl_batch_stream(gl_batch* batch, void** cuda_stream);
+int gl_batch_enqueue(gl_batch* batch, int64_t iters);
+int gl_batch_sync_status(gl_batch* batch, gl_iter_report* report);
+/* Test `index`: Res64 / zero test of its current state, its max round-off and status. */
+int gl_batch_result(gl_batch* batch, int index, gl_result* result, int* status);
+int gl_batch_get_info(const gl_batch* batch, gl_batch_info* info);
+int gl_batch_test_info(const gl_batch* batch, int index, gl_plan_info* info);
+
 /* --- no device allocation ------------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that may not call cudaMalloc (a
