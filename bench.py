@@ -316,8 +316,93 @@ def run_ours(args, world: int, rank: int, local: int):
                         "fused_max_roundoff": ef, "plain_max_roundoff": ep, "l2": "warm (continuous run)"}
         line["by_fft_length"] = by
         line["cpu_baseline"] = cpu_baseline(P3, N3)
+        if args.batched_iters > 0:
+            line["batched"] = batched_leg(gl, dev, args.batched_iters)
+        if args.serve_window > 0:
+            line["served"] = served_leg(gl, dev, args.serve_window)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def batched_leg(gl, dev: int, iters: int) -> dict:
+    """The batched configuration: 256 seeded prime exponents in [1e5, 3e6], each at the
+    smallest N = 2^a 3^b 5^c 7^d keeping <= 19.5 bits/word, advanced together for
+    `iters` iterations (one set of three launches per iteration, 64-iteration graphs).
+    Compared with the same tests run one at a time, in the plain and the fused form, from
+    each form's measured ms/iteration at each N."""
+    from gpulucas_gb300 import serve, workloads
+    ps = workloads.batch_exponents()
+    Ns = [gl.smallest_signal_size(p, 19.5) for p in ps]
+    t0 = time.perf_counter()
+    b = gl.Batch(ps, Ns, device=dev, check_every=1000)
+    build_s = time.perf_counter() - t0
+    rep = b.iterate(iters, check=False)
+    status = [b.test_status(i) for i in range(len(ps))]
+    info = b.info
+    b.close()
+    t = rep.ms * 1e-3
+    flop = sum(flop_alg(N) for N in Ns) * iters
+    pairs = list(zip(ps, Ns))
+    plain = serve.measure_ms_per_iter(pairs, gl.MODE_PLAIN, device=dev, iters=200)
+    fused = serve.measure_ms_per_iter(pairs, gl.MODE_FUSED, device=dev, iters=200)
+    seq_plain = sum(plain[N] for N in Ns) * iters * 1e-3
+    seq_fused = sum(fused[N] for N in Ns) * iters * 1e-3
+    return {
+        "workload": f"{len(ps)} primes drawn uniformly from [1e5, 3e6] (numpy default_rng(4)), smallest "
+                    f"7-smooth even N with p/N <= 19.5, {iters} iterations from S0=4",
+        "tests": len(ps), "iterations": iters, "N_range": [min(Ns), max(Ns)],
+        "seconds": t, "tests_per_h": len(ps) / t * 3600.0, "iter_s_per_test": iters / t,
+        "tflops_alg": flop / t / 1e12,
+        "max_roundoff": max(e for e, _ in status), "failed": sum(1 for _, st in status if st != 0),
+        "plan_build_s": build_s, "col_units": info.col_units, "row_units": info.row_units,
+        "gpu_launches": 3 * iters,
+        "sequential_plain_s": seq_plain, "sequential_plain_tests_per_h": len(ps) / seq_plain * 3600.0,
+        "sequential_fused_s": seq_fused, "sequential_fused_tests_per_h": len(ps) / seq_fused * 3600.0,
+        "speedup_vs_sequential_plain": seq_plain / t, "speedup_vs_sequential_fused": seq_fused / t,
+        "sequential_note": "one test at a time: sum over tests of iterations x the form's ms/iteration at "
+                           "that N, measured over 200 L2-warm iterations per distinct N (CUDA events)",
+    }
+
+
+def served_leg(gl, dev: int, window: int) -> dict:
+    """The served configuration: the first `window` requests of the seeded Poisson stream
+    (mean 50/s; 80% Res64 checks after 5000 iterations with p log-uniform in [1e5, 5e7],
+    20% full tests with p log-uniform in [1e5, 2e6]), served in real time with continuous
+    batching against a 150 GB HBM budget, each test at gl_safe_signal_size's length.  The stream is far over one GPU's capacity, so
+    the window is finite and the server runs saturated until it drains.  Compared with
+    the same requests run one at a time in arrival order (plain and fused form, from each
+    form's measured ms/iteration at each N)."""
+    from gpulucas_gb300 import serve, workloads
+    reqs = workloads.serving_requests(window)
+    srv = serve.Server(serve.GpuEngine(dev), hbm_budget_bytes=150e9)
+    done = srv.run(reqs, realtime=True)
+    ours = serve.latency_summary(done)
+    Nmap = {c.rid: c.N for c in done}
+    pairs = [(r.p, Nmap[r.rid]) for r in reqs]
+    out = {
+        "workload": f"first {window} requests of the seeded stream (numpy default_rng(5)): Poisson arrivals "
+                    "mean 50/s, 80% Res64 after k=5000 with p log-uniform prime in [1e5, 5e7], 20% full "
+                    "p-2 tests with p log-uniform prime in [1e5, 2e6]; 150 GB HBM budget; real time",
+        "requests": window, "full_tests": sum(r.full for r in reqs),
+        "errors": sum(1 for c in done if c.status != 0),
+        "restarts_at_larger_length": sum(c.attempts - 1 for c in done),
+        "length_rule": "gl_safe_signal_size: p/N <= 19.2 - 0.26 log2(N/163840)",
+        "primes_found": [c.p for c in done if c.is_prime],
+        "max_roundoff": max(c.max_roundoff for c in done),
+        "tflops_alg": srv.stats["flop"] / max(1e-9, srv.stats["busy_s"]) / 1e12,
+        "gpu_busy_frac": srv.stats["busy_s"] / srv.stats["wall_s"],
+        "peak_live": srv.stats["peak_live"], "peak_hbm_bytes": srv.stats["peak_bytes"],
+        "steps": srv.stats["steps"], "batch_rebuilds": srv.stats["rebuilds"],
+    }
+    out.update({k: v for k, v in ours.items()})
+    for name, mode in (("plain", gl.MODE_PLAIN), ("fused", gl.MODE_FUSED)):
+        ms = serve.measure_ms_per_iter(pairs, mode, device=dev, iters=200)
+        seq = serve.latency_summary(serve.sequential_schedule(reqs, lambda r: ms[Nmap[r.rid]]))
+        out[f"sequential_{name}"] = {k: seq[k] for k in ("tests_per_h", "p50_s", "p99_s", "makespan_s")}
+    out["speedup_tests_per_h_vs_sequential_plain"] = ours["tests_per_h"] / out["sequential_plain"]["tests_per_h"]
+    out["sequential_note"] = ("one test at a time in arrival order: iterations x the form's ms/iteration at "
+                              "that N, measured over 200 L2-warm iterations per distinct N (CUDA events)")
+    return out
 
 
 def plan_launches(gl) -> int:
@@ -330,6 +415,9 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--batched-iters", type=int, default=10000,
+                    help="iterations of the 256-test batched leg (0: skip)")
+    ap.add_argument("--serve-window", type=int, default=64, help="requests in the served leg (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -42,7 +42,8 @@ MODE_PLAIN = 1
 class PlanOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("device", ctypes.c_int), ("error_limit", ctypes.c_double),
                 ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
-                ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("batch_layout", ctypes.c_int),
+                ("high_priority", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -110,7 +111,12 @@ def _load():
         "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gl_smallest_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
+        "gl_safe_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
         "gl_batch_create": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
+        "gl_batch_create_from_plans": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
+        "gl_batch_query": (ctypes.c_int, [P]),
+        "gl_batch_test_status": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_int)]),
         "gl_batch_destroy": (ctypes.c_int, [P]),
         "gl_batch_iterate": (ctypes.c_int, [P, ctypes.c_int64, ctypes.POINTER(IterReport)]),
         "gl_batch_stream": (ctypes.c_int, [P, PP]),
@@ -146,7 +152,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
     "gl_checkpoint_read", "gl_plan_resume", "gl_smallest_signal_size", "gl_batch_create", "gl_batch_destroy",
     "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
-    "gl_batch_get_info", "gl_batch_test_info",
+    "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query",
 ]))
 
 
@@ -278,7 +284,14 @@ class Plan:
         return d, int(r.value), bool(z.value)
 
     def res64(self) -> int:
-        return self.residue()[1]
+        return self.res64_zero()[0]
+
+    def res64_zero(self):
+        """(res64, is_zero) of the current state; the digits stay on the device."""
+        r = ctypes.c_uint64()
+        z = ctypes.c_int()
+        _check(lib.gl_get_residue(self._h, None, ctypes.byref(r), ctypes.byref(z)), "residue")
+        return int(r.value), bool(z.value)
 
     def checkpoint_write(self, path: str):
         """Write the state in the reference's <p>.chk format (old file kept as path.bak)."""
@@ -298,7 +311,23 @@ class Plan:
 class Batch:
     """Many LL tests advanced together by one set of launches per iteration."""
 
-    def __init__(self, ps, Ns=None, **opts):
+    def __init__(self, ps=None, Ns=None, *, plans=None, **opts):
+        self._plans = None
+        if plans is not None:
+            # a batch over existing fused-form plans, which it does not own
+            plans = list(plans)
+            assert plans and ps is None and Ns is None
+            arr = (ctypes.c_void_p * len(plans))(*[pl._h.value for pl in plans])
+            o = default_opts(**opts)
+            h = ctypes.c_void_p()
+            _check(lib.gl_batch_create_from_plans(arr, len(plans), ctypes.byref(o), ctypes.byref(h)),
+                   f"batch over {len(plans)} plans")
+            self._h = h
+            self._plans = plans
+            self.ntests = len(plans)
+            self.info = BatchInfo()
+            _check(lib.gl_batch_get_info(self._h, ctypes.byref(self.info)), "batch info")
+            return
         ps = np.ascontiguousarray(ps, np.int32)
         Ns = np.zeros_like(ps) if Ns is None else np.ascontiguousarray(Ns, np.int32)
         assert ps.shape == Ns.shape and ps.ndim == 1 and ps.size > 0
@@ -338,6 +367,10 @@ class Batch:
     def enqueue(self, iters: int):
         _check(lib.gl_batch_enqueue(self._h, int(iters)), "batch enqueue")
 
+    def query(self) -> bool:
+        """True once all enqueued work has finished (does not wait)."""
+        return bool(_check(lib.gl_batch_query(self._h), "batch query"))
+
     def sync_status(self, check: bool = True) -> IterReport:
         rep = IterReport()
         st = lib.gl_batch_sync_status(self._h, ctypes.byref(rep))
@@ -356,12 +389,26 @@ class Batch:
         _check(lib.gl_batch_test_info(self._h, int(i), ctypes.byref(info)), "batch test info")
         return info
 
+    def test_status(self, i: int):
+        """(max round-off, status) of test i as of the last status read."""
+        e = ctypes.c_double()
+        st = ctypes.c_int()
+        _check(lib.gl_batch_test_status(self._h, int(i), ctypes.byref(e), ctypes.byref(st)), f"batch status {i}")
+        return e.value, st.value
+
     def result(self, i: int):
         """(Result, status) of test i."""
         r = Result()
         st = ctypes.c_int()
         _check(lib.gl_batch_result(self._h, int(i), ctypes.byref(r), ctypes.byref(st)), f"batch result {i}")
         return r, st.value
+
+
+def safe_signal_size(p: int) -> int:
+    """Smallest length whose word size keeps the measured round-off <= 0.125 (host only)."""
+    N = ctypes.c_int()
+    _check(lib.gl_safe_signal_size(int(p), ctypes.byref(N)), "safe_signal_size")
+    return N.value
 
 
 def smallest_signal_size(p: int, max_bits_per_word: float = 19.5) -> int:

@@ -22,6 +22,7 @@ struct gl_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::vector<gl_plan*> plans;
+  bool owns_plans = true;
   std::vector<void*> allocs;
   BatchLaunch launch{};
   Status* d_status = nullptr;
@@ -44,7 +45,8 @@ void free_batch(gl_batch* b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   for (void* p : b->allocs) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
-  for (gl_plan* p : b->plans) gl_plan_destroy(p);
+  if (b->owns_plans)
+    for (gl_plan* p : b->plans) gl_plan_destroy(p);
   delete b;
 }
 
@@ -54,7 +56,9 @@ int upload(gl_batch* b, T** dst, const std::vector<T>& v) {
   if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(1, v.size())) != cudaSuccess) return GL_ERR_NOMEM;
   b->allocs.push_back(p);
   b->device_bytes += sizeof(T) * v.size();
-  if (!v.empty() && cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (!v.empty() && (cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, b->stream) !=
+                         cudaSuccess ||
+                     cudaStreamSynchronize(b->stream) != cudaSuccess))
     return GL_ERR_CUDA;
   *dst = static_cast<T*>(p);
   return GL_OK;
@@ -112,61 +116,16 @@ int read_status(gl_batch* b, double* worst_err) {
   return st;
 }
 
-}  // namespace
-
-extern "C" {
-
-int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out) {
-  if (!N_out || p < 64 || !(max_bits_per_word > 1.0)) return GL_ERR_ARG;
-  const int64_t cap = 1 << 27;
-  int best = 0;
-  for (int64_t p2 = 2; p2 <= cap; p2 *= 2)
-    for (int64_t p3 = p2; p3 <= cap; p3 *= 3)
-      for (int64_t p5 = p3; p5 <= cap; p5 *= 5)
-        for (int64_t N = p5; N <= cap; N *= 7) {
-          if (N < 64 || (double)p / (double)N > max_bits_per_word) continue;
-          if (slice_depth(p, (int)N) < 0) continue;
-          if (!best || N < best) best = (int)N;
-        }
-  if (!best) return GL_ERR_SIZE;
-  *N_out = best;
-  return GL_OK;
-}
-
-int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* opts, gl_batch** out) {
-  if (!p || !out || ntests < 1) return GL_ERR_ARG;
-  *out = nullptr;
-  gl_plan_opts o;
-  if (opts) o = *opts;
-  else gl_default_opts(&o);
-  o.mode = GL_MODE_FUSED;
-  o.autotune = 0;
-  o.fft_h = 0;
-  gl_batch* b = new gl_batch();
-  b->device = o.device;
-  b->check_every = o.check_every;
-  b->error_limit = o.error_limit;
+// descriptor table, status array and unit maps of the batch's plans
+int assemble(gl_batch* b) {
+  const int ntests = (int)b->plans.size();
 #define GB_TRY(x)      \
   do {                 \
     int r_ = (x);      \
     if (r_ != GL_OK) { \
-      free_batch(b);   \
       return r_;       \
     }                  \
   } while (0)
-  if (cudaSetDevice(o.device) != cudaSuccess) {
-    delete b;
-    return GL_ERR_NODEVICE;
-  }
-  GB_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess ? GL_OK : GL_ERR_CUDA);
-  for (int i = 0; i < ntests; ++i) {
-    int n_i = N ? N[i] : 0;
-    if (n_i == 0) GB_TRY(gl_smallest_signal_size(p[i], 19.5, &n_i));
-    gl_plan* pl = nullptr;
-    GB_TRY(gl_plan_create_ex(p[i], n_i, &o, 1, &pl));
-    b->plans.push_back(pl);
-    b->device_bytes += pl->device_bytes;
-  }
   // per-test status words, one contiguous array
   std::vector<Status> zero((size_t)ntests);
   std::memset(zero.data(), 0, sizeof(Status) * zero.size());
@@ -213,8 +172,117 @@ int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* 
   b->launch.sm_col = sm_col;
   b->launch.sm_row = sm_row;
   GB_TRY(set_batch_smem_limits() == cudaSuccess ? GL_OK : GL_ERR_CUDA);
-  GB_TRY(cudaDeviceSynchronize() == cudaSuccess ? GL_OK : GL_ERR_CUDA);
 #undef GB_TRY
+  return GL_OK;
+}
+
+// smallest even N >= 64 with N/2 7-smooth, a carry depth for p/N, and p/N <= bits(N)
+template <typename Bits>
+int smallest_length(int p, Bits bits, int* N_out) {
+  const int64_t cap = 1 << 27;
+  int best = 0;
+  for (int64_t p2 = 2; p2 <= cap; p2 *= 2)
+    for (int64_t p3 = p2; p3 <= cap; p3 *= 3)
+      for (int64_t p5 = p3; p5 <= cap; p5 *= 5)
+        for (int64_t N = p5; N <= cap; N *= 7) {
+          if (N < 64 || (double)p / (double)N > bits((double)N)) continue;
+          if (slice_depth(p, (int)N) < 0) continue;
+          if (!best || N < best) best = (int)N;
+        }
+  if (!best) return GL_ERR_SIZE;
+  *N_out = best;
+  return GL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out) {
+  if (!N_out || p < 64 || !(max_bits_per_word > 1.0)) return GL_ERR_ARG;
+  return smallest_length(p, [&](double) { return max_bits_per_word; }, N_out);
+}
+
+int gl_safe_signal_size(int p, int* N_out) {
+  if (!N_out || p < 64) return GL_ERR_ARG;
+  return smallest_length(p, [](double N) { return 19.2 - 0.26 * std::log2(N / 163840.0); }, N_out);
+}
+
+int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* opts, gl_batch** out) {
+  if (!p || !out || ntests < 1) return GL_ERR_ARG;
+  *out = nullptr;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  o.mode = GL_MODE_FUSED;
+  o.autotune = 0;
+  o.fft_h = 0;
+  gl_batch* b = new gl_batch();
+  b->device = o.device;
+  b->check_every = o.check_every;
+  b->error_limit = o.error_limit;
+#define GB_TRY(x)      \
+  do {                 \
+    int r_ = (x);      \
+    if (r_ != GL_OK) { \
+      free_batch(b);   \
+      return r_;       \
+    }                  \
+  } while (0)
+  if (cudaSetDevice(o.device) != cudaSuccess) {
+    delete b;
+    return GL_ERR_NODEVICE;
+  }
+  GB_TRY(gl_make_stream(&b->stream, o.high_priority != 0) == cudaSuccess ? GL_OK : GL_ERR_CUDA);
+  for (int i = 0; i < ntests; ++i) {
+    int n_i = N ? N[i] : 0;
+    if (n_i == 0) GB_TRY(gl_smallest_signal_size(p[i], 19.5, &n_i));
+    gl_plan* pl = nullptr;
+    GB_TRY(gl_plan_create_ex(p[i], n_i, &o, 1, &pl));
+    b->plans.push_back(pl);
+    b->device_bytes += pl->device_bytes;
+  }
+  GB_TRY(assemble(b));
+#undef GB_TRY
+  *out = b;
+  return GL_OK;
+}
+
+int gl_batch_create_from_plans(gl_plan* const* plans, int nplans, const gl_plan_opts* opts, gl_batch** out) {
+  if (!plans || !out || nplans < 1) return GL_ERR_ARG;
+  *out = nullptr;
+  gl_plan_opts o;
+  if (opts) o = *opts;
+  else gl_default_opts(&o);
+  for (int i = 0; i < nplans; ++i)
+    if (!plans[i] || plans[i]->mode != GL_MODE_FUSED || plans[i]->device != plans[0]->device) return GL_ERR_ARG;
+  // a pending state load (after gl_set_carry_state / gl_plan_resume) is consumed by the
+  // plan's own next iteration; the batch's kernels start from the products
+  for (int i = 0; i < nplans; ++i)
+    if (plans[i]->from_state) return GL_ERR_STATE;
+  gl_batch* b = new gl_batch();
+  b->owns_plans = false;
+  b->device = plans[0]->device;
+  b->check_every = o.check_every;
+  b->error_limit = o.error_limit;
+  if (cudaSetDevice(b->device) != cudaSuccess ||
+      gl_make_stream(&b->stream, o.high_priority != 0) != cudaSuccess) {
+    free_batch(b);
+    return GL_ERR_CUDA;
+  }
+  for (int i = 0; i < nplans; ++i) {
+    b->plans.push_back(plans[i]);
+    // the batch's kernels must see each plan's pending work
+    if (cudaStreamSynchronize(plans[i]->stream) != cudaSuccess) {
+      free_batch(b);
+      return GL_ERR_CUDA;
+    }
+  }
+  const int rc = assemble(b);
+  if (rc != GL_OK) {
+    free_batch(b);
+    return rc;
+  }
   *out = b;
   return GL_OK;
 }
@@ -289,6 +357,14 @@ int gl_batch_sync_status(gl_batch* b, gl_iter_report* rep) {
   return st;
 }
 
+int gl_batch_query(gl_batch* b) {
+  if (!b) return GL_ERR_ARG;
+  const cudaError_t e = cudaStreamQuery(b->stream);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return GL_ERR_CUDA;
+}
+
 int gl_batch_result(gl_batch* b, int index, gl_result* r, int* status) {
   if (!b || !r || index < 0 || index >= (int)b->plans.size()) return GL_ERR_ARG;
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return GL_ERR_CUDA;
@@ -309,6 +385,15 @@ int gl_batch_result(gl_batch* b, int index, gl_result* r, int* status) {
     const Status& s = b->h_status[(size_t)index];
     *status = s.flags ? GL_ERR_OVERFLOW : (b->maxerr[(size_t)index] >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK);
   }
+  return GL_OK;
+}
+
+int gl_batch_test_status(const gl_batch* b, int index, double* max_roundoff, int* status) {
+  if (!b || index < 0 || index >= (int)b->plans.size()) return GL_ERR_ARG;
+  const double e = b->maxerr[(size_t)index];
+  if (max_roundoff) *max_roundoff = e;
+  if (status)
+    *status = b->h_status[(size_t)index].flags ? GL_ERR_OVERFLOW : (e >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK);
   return GL_OK;
 }
 

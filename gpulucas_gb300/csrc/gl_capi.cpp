@@ -402,10 +402,19 @@ int setSliceAndDice(int testPrime, int signalSize) {
 }
 
 int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
-  return gl_plan_create_ex(p, N, opts, 0, out);
+  return gl_plan_create_ex(p, N, opts, opts && opts->batch_layout ? 1 : 0, out);
 }
 
 }  // extern "C"
+
+cudaError_t gl_make_stream(cudaStream_t* s, bool high) {
+  int least = 0, greatest = 0;
+  if (high) {
+    const cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, high ? greatest : least);
+}
 
 void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters) {
   pl->iters_done += iters;
@@ -467,7 +476,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   } while (0)
 #define GL_TRYC(x) GL_TRY(cuda_status(x))
 
-  GL_TRYC(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+  GL_TRYC(gl_make_stream(&pl->stream, o.high_priority != 0));
   GL_TRYC(cudaEventCreate(&pl->ev0));
   GL_TRYC(cudaEventCreate(&pl->ev1));
   GL_TRYC(cudaMallocHost((void**)&pl->h_status, sizeof(Status)));
@@ -508,11 +517,12 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     GL_TRY(dev_alloc(pl, &Z2, M));
     GL_TRY(dev_alloc(pl, &dtwM, M));
     GL_TRY(dev_alloc(pl, &dPair, M));
-    GL_TRYC(cudaMemcpy(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dPair, pc.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(fl, flags.data(), N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpyAsync(dtwM, twM.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dPair, pc.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(fl, flags.data(), N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dA, A.data(), sizeof(double) * N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dAi, Ainv.data(), sizeof(double) * N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaStreamSynchronize(pl->stream));  // host tables go out of scope
   } else {
     const int W = fg.W, H = fg.H;
     // per-word tables in column-major order: word j = 2(m1 + W m2) + e -> 2(m1 H + m2) + e
@@ -548,15 +558,16 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     GL_TRY(dev_alloc(pl, &dK1, M));
     GL_TRY(dev_alloc(pl, &dPair, M));
     GL_TRY(dev_alloc(pl, &dK2, M));
-    GL_TRYC(cudaMemcpy(fl, fl_c.data(), N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(span, span_c.data(), N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dA, A_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dAi, Ai_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dtwW, twW.data(), sizeof(DevCplx) * twW.size(), cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dtwH, twH.data(), sizeof(DevCplx) * twH.size(), cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dK1, tK1.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dPair, tPair.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
-    GL_TRYC(cudaMemcpy(dK2, tK2.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice));
+    GL_TRYC(cudaMemcpyAsync(fl, fl_c.data(), N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(span, span_c.data(), N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dA, A_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dAi, Ai_c.data(), sizeof(double) * N, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dtwW, twW.data(), sizeof(DevCplx) * twW.size(), cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dtwH, twH.data(), sizeof(DevCplx) * twH.size(), cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dK1, tK1.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dPair, tPair.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaMemcpyAsync(dK2, tK2.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
+    GL_TRYC(cudaStreamSynchronize(pl->stream));  // host tables go out of scope
     a.W = W; a.H = H; a.G = 1; a.pw = pl->fg.pw; a.ph = pl->fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
     GL_TRYC(set_fused_smem_limits(fg));
   }
@@ -593,6 +604,7 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
   if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && o.device >= 0 && o.device < ndev)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device);
   if (sms <= 0) sms = 152;  // GB300
+  if (o.batch_layout) sms = 1;
   int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg)
                                    : choose_plain_geom(tmp.M, &tmp.pg);
   if (rc != GL_OK) return rc;
@@ -600,9 +612,10 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
   int r = gl_plan_get_info(&tmp, info);
   if (o.mode == GL_MODE_FUSED) {
     const size_t M = tmp.M, N8 = (size_t)N * 8;
+    const size_t stages = (size_t)stage_offsets(tmp.fg.pw, tmp.fg.pw.off) + stage_offsets(tmp.fg.ph, tmp.fg.ph.off);
     info->device_bytes = N8 /*ll*/ + 2 * (size_t)N /*flags, span*/ + 2 * N8 /*A, Ainv*/ +
-                         4 * M * 16 /*Z, 3 twiddle tables*/ + (size_t)(tmp.fg.W + tmp.fg.H) * 16 +
-                         (size_t)N * 5 /*digit, hi*/ + 16;
+                         4 * M * 16 /*Z, 3 twiddle tables*/ + stages * 16 + (size_t)N * 5 /*digit, hi*/ +
+                         sizeof(Status);
   }
   return r;
 }

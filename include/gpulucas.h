@@ -52,7 +52,10 @@ typedef struct {
     int fft_h;             /* 0 = automatic; else force the column length H of M = W*H */
     int cols_per_cta;      /* 0 or 1 (the column passes take one column per CTA) */
     int autotune;          /* 1 (default): time the best few layouts once per N per process */
-    int reserved[7];
+    int batch_layout;      /* 1: layout for running inside a batch (total work, no timing) */
+    int high_priority;     /* 1: the plan's (or batch's) stream gets the device's highest
+                              priority, so its blocks are scheduled ahead of other work */
+    int reserved[5];
 } gl_plan_opts;
 
 typedef struct {
@@ -181,6 +184,12 @@ int gl_mersenne_test(gl_plan* plan, int64_t iters, gl_result* result);
  * N/2 = 2^a 3^b 5^c 7^d (any exponents) and p/N <= max_bits_per_word (the batch
  * configuration uses 19.5). */
 int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out);
+/* Smallest such N with p/N <= 19.2 - 0.26 log2(N / 163840): the word size at which the
+ * fused kernels' measured max round-off over 300 iterations from S0 = 4 stays at or
+ * below 0.125 on GB300 (5760 <= N <= 2621440), leaving the 0.4 limit a factor three for
+ * the tail of long runs.  A host-only length rule for servers that cannot afford
+ * gl_find_signal_size's trial runs. */
+int gl_safe_signal_size(int p, int* N_out);
 
 typedef struct gl_batch gl_batch;
 typedef struct {
@@ -197,6 +206,11 @@ typedef struct {
  * advance every test by one iteration (64-iteration CUDA graphs).  opts: device,
  * error_limit, check_every. */
 int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* opts, gl_batch** batch);
+/* A batch over existing fused-form plans of the same device, which it does not own: a
+ * server rebuilds the batch when its set of live tests changes without rebuilding any
+ * test's tables.  The plans must outlive the batch and are advanced only through it
+ * while it exists. */
+int gl_batch_create_from_plans(gl_plan* const* plans, int nplans, const gl_plan_opts* opts, gl_batch** batch);
 int gl_batch_destroy(gl_batch* batch);
 /* All tests advance `iters` iterations; per-test round-off is checked every check_every.
  * Returns the worst status (GL_ERR_ROUNDOFF / GL_ERR_OVERFLOW name some test). */
@@ -204,8 +218,13 @@ int gl_batch_iterate(gl_batch* batch, int64_t iters, gl_iter_report* report);
 int gl_batch_stream(gl_batch* batch, void** cuda_stream);
 int gl_batch_enqueue(gl_batch* batch, int64_t iters);
 int gl_batch_sync_status(gl_batch* batch, gl_iter_report* report);
+/* 1 if everything enqueued on the batch has finished, 0 if not, < 0 on error (no wait). */
+int gl_batch_query(gl_batch* batch);
 /* Test `index`: Res64 / zero test of its current state, its max round-off and status. */
 int gl_batch_result(gl_batch* batch, int index, gl_result* result, int* status);
+/* Round-off and status of one test as of the last status read (gl_batch_iterate or
+ * gl_batch_sync_status); no device work. */
+int gl_batch_test_status(const gl_batch* batch, int index, double* max_roundoff, int* status);
 int gl_batch_get_info(const gl_batch* batch, gl_batch_info* info);
 int gl_batch_test_info(const gl_batch* batch, int index, gl_plan_info* info);
 
