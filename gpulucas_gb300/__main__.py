@@ -1,6 +1,7 @@
 """Command line with the reference's flags (gpuLucas.cu:374-454):
 
-    python -m gpulucas_gb300 [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] [p]
+    python -m gpulucas_gb300 [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain]
+                             [-H h] [p]
 
 -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); without -f the length is chosen as
         findSignalSize does (gpuLucas.cu:1064-1187)
@@ -10,6 +11,7 @@
         (gpuLucas.cu:1414-1423); a run finding <p>.chk or <p>.chk.bak resumes from it
 -k k    stop after k iterations and print Res64 (0 = full p-2 test)
 -m      execution form: fused (default) or plain
+-H h    fused form: FFT column length h (M = h x w), instead of the timed layout search
 SIGINT / SIGTERM write a checkpoint and exit (gpuLucas.cu:365-369, 1425-1429).
 A full test appends the reference's result line to results.txt (gpuLucas.cu:1514-1548)
 and removes its checkpoint files (gpuLucas.cu:628-632).
@@ -41,6 +43,7 @@ def main(argv=None) -> int:
     ap.add_argument("-c", type=int, default=0)
     ap.add_argument("-k", type=int, default=0)
     ap.add_argument("-m", choices=["fused", "plain"], default="fused")
+    ap.add_argument("-H", type=int, default=0)
     ap.add_argument("p", nargs="?", type=int, default=0)
     a = ap.parse_args(argv)
     if a.h:
@@ -74,7 +77,7 @@ def main(argv=None) -> int:
     signal.signal(signal.SIGINT, _on_signal)
     signal.signal(signal.SIGTERM, _on_signal)
     t0 = time.time()
-    with gl.Plan(p, N, mode=mode, device=a.d) as pl:
+    with gl.Plan(p, N, mode=mode, device=a.d, fft_h=a.H) as pl:
         i = pl.info
         if resume_k is not None:
             pl.resume(chk)
