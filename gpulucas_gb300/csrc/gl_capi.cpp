@@ -241,6 +241,7 @@ void free_plan(gl_plan* pl) {
   if (pl->gexec) cudaGraphExecDestroy(pl->gexec);
   for (void* p : pl->allocs) cudaFree(p);
   if (pl->h_status) cudaFreeHost(pl->h_status);
+  if (pl->h_res) cudaFreeHost(pl->h_res);
   if (pl->ev0) cudaEventDestroy(pl->ev0);
   if (pl->ev1) cudaEventDestroy(pl->ev1);
   if (pl->stream) cudaStreamDestroy(pl->stream);
@@ -309,55 +310,6 @@ int read_status(gl_plan* pl, double* maxerr_out) {
 
 // Host side of addPseudoBalanced + rebalanceIrrIntSEQGPU (IrrBaseBalanced.cu:117-169):
 // one balanced carry pass with the final carry wrapped into word 0.
-void rebalance_host(const gl_plan* pl, const std::vector<int32_t>& bits, const int32_t* digit, const int8_t* hi,
-                    int32_t* out) {
-  const int N = pl->N;
-  for (int j = 0; j < N; ++j) out[j] = digit[j] + hi[j == 0 ? N - 1 : j - 1];
-  int carry = 0;
-  for (int j = 0; j < N; ++j) {
-    const int base = 1 << bits[j], half = base >> 1;
-    const int t = out[j] + carry;
-    if (t >= half) { out[j] = t - base; carry = 1; }
-    else if (t < -half) { out[j] = t + base; carry = -1; }
-    else { out[j] = t; carry = 0; }
-  }
-  if (carry) out[0] += carry;
-}
-
-// Canonical non-negative digits of the value mod 2^p - 1 (floor carries, the carry
-// out of the top word re-enters at word 0 since 2^p == 1), then the low 64 bits
-// (print_residue, gpuLucas.cu:1288-1352).  Returns 1 if the value is 0 mod 2^p - 1.
-int residue_host(const gl_plan* pl, const std::vector<int32_t>& bits, const int32_t* balanced, uint64_t* res64) {
-  const int N = pl->N;
-  std::vector<int64_t> d(balanced, balanced + N);
-  for (int pass = 0; pass < 8; ++pass) {
-    int64_t carry = 0;
-    for (int j = 0; j < N; ++j) {
-      const int64_t base = (int64_t)1 << bits[j];
-      int64_t v = d[j] + carry;
-      int64_t q = v >= 0 ? v >> bits[j] : -((-v + base - 1) >> bits[j]);
-      d[j] = v - q * base;
-      carry = q;
-    }
-    if (carry == 0) break;
-    d[0] += carry;
-  }
-  bool all0 = true, allmax = true;
-  for (int j = 0; j < N; ++j) {
-    if (d[j] != 0) all0 = false;
-    if (d[j] != ((int64_t)1 << bits[j]) - 1) allmax = false;
-  }
-  uint64_t r = 0;
-  int pos = 0;
-  for (int j = 0; j < N && pos < 64; ++j) {
-    r |= (uint64_t)d[j] << pos;  // bits above 64 fall off
-    pos += bits[j];
-  }
-  if (allmax) r = 0;
-  *res64 = r;
-  return (all0 || allmax) ? 1 : 0;
-}
-
 }  // namespace
 
 extern "C" {
@@ -509,6 +461,8 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   GL_TRY(dev_alloc(pl, &digit, N));
   GL_TRY(dev_alloc(pl, &hi, N));
   GL_TRY(dev_alloc(pl, &status, 1));
+  GL_TRY(dev_alloc(pl, &pl->rscratch, residue_scratch_bytes(N)));
+  GL_TRYC(cudaMallocHost((void**)&pl->h_res, sizeof(int32_t) * 72));
   if (o.mode == GL_MODE_PLAIN) {
     std::vector<HostCplx> pc((size_t)M);
     parallel_for(M, [&](int64_t b, int64_t e) {
@@ -615,7 +569,7 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
     const size_t stages = (size_t)stage_offsets(tmp.fg.pw, tmp.fg.pw.off) + stage_offsets(tmp.fg.ph, tmp.fg.ph.off);
     info->device_bytes = N8 /*ll*/ + 2 * (size_t)N /*flags, span*/ + 2 * N8 /*A, Ainv*/ +
                          4 * M * 16 /*Z, 3 twiddle tables*/ + stages * 16 + (size_t)N * 5 /*digit, hi*/ +
-                         sizeof(Status);
+                         sizeof(Status) + residue_scratch_bytes(N);
   }
   return r;
 }
@@ -844,18 +798,34 @@ int gl_set_carry_state(gl_plan* pl, const int32_t* digit, const int8_t* hi, int6
 
 int gl_get_residue(gl_plan* pl, int32_t* digits_out, uint64_t* res64, int* is_zero) {
   if (!pl) return GL_ERR_ARG;
-  std::vector<int32_t> digit(pl->N), out(pl->N), bits;
-  std::vector<int8_t> hi(pl->N);
-  std::vector<uint8_t> flags;
-  int rc = gl_get_carry_state(pl, digit.data(), hi.data());
+  GL_CUDA(cudaSetDevice(pl->device));
+  int rc = ensure_carry(pl);
   if (rc != GL_OK) return rc;
-  word_tables(pl->p, pl->N, bits, flags);
-  rebalance_host(pl, bits, digit.data(), hi.data(), out.data());
-  if (digits_out) std::memcpy(digits_out, out.data(), sizeof(int32_t) * pl->N);
+  // the work array is idle between iterations: it holds the balanced digits
+  int32_t* balanced = reinterpret_cast<int32_t*>(pl->args.Z);
+  GL_CUDA(launch_residue(pl->args, pl->mode == GL_MODE_FUSED, balanced, pl->rscratch, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->h_res, pl->rscratch + residue_head_offset(pl->N), sizeof(int32_t) * 69,
+                          cudaMemcpyDeviceToHost, pl->stream));
+  if (digits_out)
+    GL_CUDA(cudaMemcpyAsync(digits_out, balanced, sizeof(int32_t) * pl->N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaStreamSynchronize(pl->stream));
+  const int32_t* head = pl->h_res;
+  const int32_t* scal = head + 64;
+  const int flags = head[68];
+  if (scal[2] != scal[3]) return GL_ERR_STATE;  // the end-around carry has no fixed point
+  const bool all0 = !(flags & 1), allmax = !(flags & 2);
+  // low 64 bits of the canonical digits; word j holds ceil(p(j+1)/N) - ceil(pj/N) bits
   uint64_t r = 0;
-  int z = residue_host(pl, bits, out.data(), &r);
+  int pos = 0;
+  for (int j = 0; j < pl->N && j < 64 && pos < 64; ++j) {
+    const int64_t lo = ((int64_t)pl->p * j + pl->N - 1) / pl->N;
+    const int64_t hi = ((int64_t)pl->p * (j + 1) + pl->N - 1) / pl->N;
+    r |= (uint64_t)(uint32_t)head[j] << pos;  // bits above 64 fall off
+    pos += (int)(hi - lo);
+  }
+  if (allmax) r = 0;  // 2^p - 1 == 0
   if (res64) *res64 = r;
-  if (is_zero) *is_zero = z;
+  if (is_zero) *is_zero = (all0 || allmax) ? 1 : 0;
   return GL_OK;
 }
 

@@ -110,6 +110,16 @@ cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long l
 cudaError_t set_fused_smem_limits(const FusedGeom& g);
 cudaError_t set_batch_smem_limits();
 cudaError_t launch_batch_iteration(const BatchLaunch& b, cudaStream_t s, bool from_state);
+
+// End-of-run normalisation on the device (gl_residue.cu): from the carry-save state
+// (digit, hi) the reference's balanced rebalance into `balanced` (N words), then the
+// canonical digits' first 64 words, the carries into word 0 and the zero flags into
+// `scratch` (residue_scratch_bytes(N) bytes; head at residue_head_offset(N): int32
+// head[64], scal[4], flags).  colmajor_flags: the flags table is in the fused layout.
+size_t residue_scratch_bytes(int N);
+size_t residue_head_offset(int N);
+cudaError_t launch_residue(const IterArgs& a, bool colmajor_flags, int32_t* balanced, void* scratch,
+                           cudaStream_t s);
 cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s);
 
 }  // namespace gl

@@ -30,6 +30,8 @@ struct gl_plan {
   int gexec_iters = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t device_bytes = 0;
+  uint8_t* rscratch = nullptr;  // device scratch of the residue kernels
+  int32_t* h_res = nullptr;     // pinned: 64 canonical head digits, scalars, flags
 };
 
 

@@ -47,6 +47,50 @@ def test_products_and_carry_state_match_oracle(gl, orc, p, N, mode):
         assert r == orc.Exact(p).iterate(done).res64()
 
 
+def _carry_states(orc, p, N, rng):
+    """Random balanced states and the edge cases of the carry chains."""
+    b, _ = orc.bits(p, N)
+    b = b.astype(np.int64)
+    half = (1 << (b - 1)).astype(np.int64)
+    yield "random", rng.integers(-half, half).astype(np.int32), rng.integers(-128, 128, N).astype(np.int8)
+    yield "zero", np.zeros(N, np.int32), np.zeros(N, np.int8)
+    yield "all max (2^p - 1)", ((1 << b) - 1).astype(np.int32), np.zeros(N, np.int8)
+    d = np.zeros(N, np.int32)
+    d[0] = -1
+    yield "minus one", d, np.zeros(N, np.int8)
+    d = np.where(rng.random(N) < 0.95, half - 1, -half).astype(np.int32)
+    yield "long chains", d, rng.integers(-2, 3, N).astype(np.int8)
+    yield "all negative", (-half).astype(np.int32), np.full(N, -1, np.int8)
+    d = np.zeros(N, np.int32)
+    d[N - 1] = -1
+    yield "borrow wraps", d, np.zeros(N, np.int8)
+
+
+@pytest.mark.parametrize("p,N", [(44497, 2048), (4423, 256), (1000003, 54432), (2976221, 163840),
+                                 (43112609, 2359296)])
+@pytest.mark.parametrize("mode", [0, 1], ids=["fused", "plain"])
+def test_device_residue_matches_oracle(gl, orc, p, N, mode):
+    """The device normalisation (balanced rebalance, canonical digits, Res64, zero test)
+    against the oracle's restatement of rebalanceIrrIntSEQGPU (inner.cu:133-169) and
+    print_residue (gpuLucas.cu:1288-1352) on arbitrary carry-save states.  N = 2359296
+    spans 1152 blocks of the scan, more than one pass of the one-block scan."""
+    rng = np.random.default_rng(N + mode)
+    with gl.Plan(p, N, mode=mode) as pl:
+        for name, d, h in _carry_states(orc, p, N, rng):
+            if N > 200000 and name not in ("random", "all max (2^p - 1)", "borrow wraps"):
+                continue
+            pl.set_carry_state(d, h, 7)
+            digits, r, z = pl.residue()
+            ref = orc.rebalance(p, N, d, h)
+            assert (digits == ref).all(), (name, np.nonzero(digits != ref)[0][:8])
+            exact_zero = name in ("zero", "all max (2^p - 1)")   # by construction
+            if N <= 4096:
+                assert (orc.digits_to_int(p, N, ref) == 0) == exact_zero
+            assert z == exact_zero, name
+            assert r == (0 if exact_zero else orc.res64_normalize(p, N, ref)), name
+            assert pl.res64_zero() == (r, z)
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432)])
 def test_dice_through_abi(gl, orc, p, N):
     """llintToBalInt<n> semantics on arbitrary products via gl_set_products."""
