@@ -374,7 +374,7 @@ def served_leg(gl, dev: int, window: int) -> dict:
     form's measured ms/iteration at each N)."""
     from gpulucas_gb300 import serve, workloads
     reqs = workloads.serving_requests(window)
-    srv = serve.Server(serve.GpuEngine(dev), hbm_budget_bytes=150e9)
+    srv = serve.Server(device=dev, hbm_budget_bytes=150e9)
     done = srv.run(reqs, realtime=True)
     ours = serve.latency_summary(done)
     Nmap = {c.rid: c.N for c in done}
@@ -389,10 +389,9 @@ def served_leg(gl, dev: int, window: int) -> dict:
         "length_rule": "gl_safe_signal_size: p/N <= 19.2 - 0.26 log2(N/163840)",
         "primes_found": [c.p for c in done if c.is_prime],
         "max_roundoff": max(c.max_roundoff for c in done),
-        "tflops_alg": srv.stats["flop"] / max(1e-9, srv.stats["busy_s"]) / 1e12,
-        "gpu_busy_frac": srv.stats["busy_s"] / srv.stats["wall_s"],
+        "tflops_alg": srv.stats["flop"] / srv.stats["wall_s"] / 1e12,
         "peak_live": srv.stats["peak_live"], "peak_hbm_bytes": srv.stats["peak_bytes"],
-        "steps": srv.stats["steps"], "batch_rebuilds": srv.stats["rebuilds"],
+        "steps": srv.stats["steps"], "batch_rebuilds": srv.stats["rebuilds"], "lanes": srv.stats["lanes"],
     }
     out.update({k: v for k, v in ours.items()})
     for name, mode in (("plain", gl.MODE_PLAIN), ("fused", gl.MODE_FUSED)):

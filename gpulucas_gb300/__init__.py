@@ -60,6 +60,57 @@ class BatchInfo(ctypes.Structure):
                 ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t), ("iterations", ctypes.c_int64)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double), ("max_active", ctypes.c_int),
+                ("step_ms", ctypes.c_double), ("checkpoint_every", ctypes.c_int64),
+                ("max_bits_per_word", ctypes.c_double), ("retries", ctypes.c_int),
+                ("chain_iterations", ctypes.c_int64), ("lanes", ctypes.c_int), ("build_threads", ctypes.c_int),
+                ("error_limit", ctypes.c_double), ("check_every", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("p", ctypes.c_int), ("N", ctypes.c_int), ("iterations", ctypes.c_int64),
+                ("full", ctypes.c_int), ("status", ctypes.c_int), ("is_zero", ctypes.c_int),
+                ("is_prime", ctypes.c_int), ("res64", ctypes.c_uint64), ("max_roundoff", ctypes.c_double),
+                ("arrival_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("attempts", ctypes.c_int), ("lane", ctypes.c_int), ("n_checkpoints", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("wall_s", ctypes.c_double), ("lane_busy_s", ctypes.c_double * 2), ("steps", ctypes.c_int64 * 2),
+                ("rebuilds", ctypes.c_int64 * 2), ("peak_live", ctypes.c_int * 2), ("live", ctypes.c_int),
+                ("queued", ctypes.c_int), ("building", ctypes.c_int), ("bytes_in_use", ctypes.c_size_t),
+                ("peak_bytes", ctypes.c_size_t), ("flop_alg", ctypes.c_double), ("submitted", ctypes.c_int64),
+                ("completed", ctypes.c_int64)]
+
+
+# callbacks of gl_server_engine
+ENGINE_SIGNAL_SIZE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_int))
+ENGINE_FOOTPRINT = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_size_t))
+ENGINE_CREATE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_void_p))
+ENGINE_DESTROY = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
+ENGINE_BATCH = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                ctypes.c_int, ctypes.POINTER(ctypes.c_void_p))
+ENGINE_CLOSE_BATCH = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p)
+ENGINE_START = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64)
+ENGINE_READY = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
+ENGINE_FINISH = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int))
+ENGINE_RES64 = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                ctypes.POINTER(ctypes.c_int))
+
+
+class ServerEngine(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("signal_size", ENGINE_SIGNAL_SIZE), ("footprint", ENGINE_FOOTPRINT),
+                ("create", ENGINE_CREATE), ("destroy", ENGINE_DESTROY), ("batch", ENGINE_BATCH),
+                ("close_batch", ENGINE_CLOSE_BATCH), ("start", ENGINE_START), ("ready", ENGINE_READY),
+                ("finish", ENGINE_FINISH), ("res64", ENGINE_RES64)]
+
+
 class IterReport(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("total_iterations", ctypes.c_int64),
                 ("max_roundoff", ctypes.c_double), ("ms", ctypes.c_double), ("status", ctypes.c_int)]
@@ -129,6 +180,17 @@ def _load():
         "gl_checkpoint_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                               ctypes.POINTER(ctypes.c_int64), vp]),
         "gl_plan_resume": (ctypes.c_int, [P, ctypes.c_char_p]),
+        "gl_server_default_opts": (ctypes.c_int, [ctypes.POINTER(ServerOpts)]),
+        "gl_server_create": (ctypes.c_int, [ctypes.POINTER(ServerOpts), ctypes.POINTER(ServerEngine), PP]),
+        "gl_server_submit": (ctypes.c_int, [P, ctypes.c_int64, ctypes.c_int, ctypes.c_int64]),
+        "gl_server_poll": (ctypes.c_int, [P, ctypes.POINTER(Completion), ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.c_double]),
+        "gl_server_drain": (ctypes.c_int, [P]),
+        "gl_server_checkpoints": (ctypes.c_int, [P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
+                                                 ctypes.POINTER(ctypes.c_uint64), ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_int)]),
+        "gl_server_get_stats": (ctypes.c_int, [P, ctypes.POINTER(ServerStats)]),
+        "gl_server_destroy": (ctypes.c_int, [P]),
         "gl_iterate_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int64,
                                               ctypes.POINTER(ctypes.c_double), vp]),
     }
@@ -153,6 +215,8 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_checkpoint_read", "gl_plan_resume", "gl_smallest_signal_size", "gl_batch_create", "gl_batch_destroy",
     "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
     "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query",
+    "gl_server_default_opts", "gl_server_create", "gl_server_submit", "gl_server_poll", "gl_server_drain",
+    "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy",
 ]))
 
 

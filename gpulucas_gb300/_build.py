@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgpulucas_gb300.so")
 HOSTCHECK = os.path.join(HERE, "libgl_hostcheck.so")
 
-SOURCES = ["gl_kernels.cu", "gl_residue.cu", "gl_capi.cpp", "gl_tables.cpp", "gl_noalloc.cu", "gl_checkpoint.cpp",
+SOURCES = ["gl_kernels.cu", "gl_residue.cu", "gl_capi.cpp", "gl_tables.cpp", "gl_noalloc.cu", "gl_checkpoint.cpp", "gl_server.cpp",
            "gl_batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

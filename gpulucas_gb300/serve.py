@@ -1,47 +1,36 @@
-"""Serving loop: continuous batching of Lucas-Lehmer requests on one GPU.
+"""Serving: continuous batching of Lucas-Lehmer requests on one GPU.
 
-A request asks for the Res64 of 2^p - 1 after k iterations from S0 = 4, or for a full
-p - 2 test.  Requests arrive over time; the server
+The request loop is the library's C++ server (gl_server_* in include/gpulucas.h): a
+background thread admits submitted requests against an HBM budget and a slot limit,
+builds each test's plan on worker threads, and advances the live tests in two batches on
+two streams -- the chain lane (the device's highest stream priority) for full tests and
+long requests, whose latency is a chain of dependent iterations too small to fill the
+GPU, and the bulk lane for the rest, which soaks up the SMs the chain lane leaves idle.
+A lane's batch is rebuilt from the live plans when its membership changes; every step is
+bounded by `step_ms` of GPU time and by the next completion or Res64 checkpoint, so an
+arrival waits at most one step.  A test whose round-off reaches the limit restarts from
+S0 = 4 at the next larger FFT length (the reference aborts such a run,
+gpuLucas.cu:1470-1479).  Residues stay on the device; a finished test reports its Res64
+and zero test and frees its memory.
 
-* admits queued requests in arrival order while the number of live tests is below
-  `max_active` and their device footprint (as `describe` predicts it) fits the HBM
-  budget; a test's tables are built on a worker thread while the GPU runs the others;
-* keeps every live test's state on the device and advances the live tests together, one
-  set of batched launches per iteration (a gl_batch over the live plans, rebuilt only when
-  the live set changes; the plans and their state are not touched by a rebuild);
-* runs two such batches side by side on two streams.  The chain lane (a stream at the
-  device's highest priority) holds the tests with long iteration chains (full tests and
-  any request of more than `chain_iterations`): their latency is a chain of dependent
-  iterations, each too small to fill the GPU, so their blocks are scheduled first.  The
-  bulk lane holds the rest and soaks up the SMs the chain lane leaves idle;
-* steps each lane by at most `step_ms` of GPU time, never past the next completion or
-  Res64 checkpoint of its tests, so arrivals wait at most one step to be admitted;
-* checks every live test's round-off after each step: a test at or above the limit stops,
-  as the reference aborts (gpuLucas.cu:1470-1479), and is queued again from S0 = 4 at the
-  next larger FFT length (at most `retries` times, then retired with GL_ERR_ROUNDOFF);
-* records the Res64 of full tests every `checkpoint_every` iterations, and retires
-  finished tests with their Res64 / zero test, freeing their memory for the queue.
-
-FFT lengths come from gl_safe_signal_size (a host rule calibrated on the fused kernels'
-measured round-off), or from a fixed bits/word bound when `max_bits_per_word` is given.
+This module drives that server from Python: `Server.run` submits a request list in real
+time (each request at its arrival time) or all at once, and collects the completions.
+An engine object (see `PyEngine`) can stand in for the GPU so the scheduling logic runs
+on the CPU in the tests.  The reference runs one test per process (gpuLucas.cu:374-639)
+and has no server.
 
 Results do not depend on co-scheduling: each test keeps its own tables and state, the
 batched kernels compute exactly what the test's own fused kernels compute, and the
 integer products after rounding do not depend on the FFT layout while the round-off
 stays below 0.5.
-
-The reference runs one test per process (gpuLucas.cu:374-639) and has no server; this
-module is the served configuration of this library.  The engine behind the loop is a
-small interface (`GpuEngine` here) so the scheduling logic can be exercised on the CPU
-with an exact integer engine in the tests.
 """
 from __future__ import annotations
 
+import ctypes
+import itertools
 import math
 import statistics
 import time
-from collections import deque
-from concurrent.futures import Future, ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Callable, Iterable, Sequence
 
@@ -50,6 +39,7 @@ from .workloads import Request
 GL_OK = 0
 GL_ERR_NOMEM = -5      # request can never fit the HBM budget
 GL_ERR_ROUNDOFF = -6
+GL_ERR_STATE = -11
 
 
 def flop_alg(N: int) -> float:
@@ -81,278 +71,172 @@ class Completion:
         return self.done_s - self.arrival_s
 
 
-@dataclass
-class _Live:
-    req: Request
-    N: int
-    nbytes: int
-    admit_s: float
-    handle: object = None
-    future: Future | None = None
-    done: int = 0
-    maxerr: float = 0.0
-    checkpoints: list = field(default_factory=list)
-    attempts: int = 1
+class PyEngine:
+    """A gl_server_engine whose calls go to a Python object with the methods
+    signal_size(p, max_bits_per_word | None, above) -> N, footprint(p, N) -> bytes,
+    create(p, N) -> test, destroy(test), batch(tests, high_priority) -> batch,
+    close_batch(batch), start(batch, iters), ready(batch) -> bool,
+    finish(batch) -> [(max_roundoff, status)] in test order, res64(test) -> (res64, is_zero).
+    Objects are passed to the server as integer handles."""
 
-
-class GpuEngine:
-    """The library's fused-form plans and batches on one device."""
-
-    def __init__(self, device: int = 0, check_every: int = 1000, error_limit: float = 0.4, batch_layout: int = 0):
-        """batch_layout=0: each test keeps the layout it would have alone (cost model for
-        the whole device), so a test left running alone is not slowed down; 1: the layout
-        with the least total work."""
+    def __init__(self, impl):
         import gpulucas_gb300 as gl
         self.gl = gl
-        self.device = device
-        self.layout = dict(batch_layout=int(batch_layout), autotune=0)
-        self.opts = dict(device=device, check_every=check_every, error_limit=error_limit)
+        self.impl = impl
+        self.objs: dict[int, object] = {}
+        self.ids = itertools.count(1)   # callbacks come from several server threads
+        self.error: BaseException | None = None
 
-    def signal_size(self, p: int, max_bits_per_word: float | None, above: int = 0) -> int:
-        """Length for p (larger than `above` when given)."""
-        if above:
-            return self.gl.smallest_signal_size(p, p / (above + 1.0))
-        if max_bits_per_word is None:
-            return self.gl.safe_signal_size(p)
-        return self.gl.smallest_signal_size(p, max_bits_per_word)
+        def guard(fn, fail=GL_ERR_STATE):
+            def wrapped(*a):
+                try:
+                    return fn(*a)
+                except BaseException as e:  # noqa: BLE001 - reported after the run
+                    if self.error is None:
+                        self.error = e
+                    return fail
+            return wrapped
 
-    def footprint(self, p: int, N: int) -> int:
-        return int(self.gl.describe(p, N, device=self.device, **self.layout).device_bytes)
+        def put(obj) -> int:
+            h = next(self.ids)
+            self.objs[h] = obj
+            return h
 
-    def create(self, p: int, N: int):
-        pl = self.gl.Plan(p, N, **self.layout, **self.opts)
-        pl.reset()
-        return pl
+        def signal_size(ctx, p, bits, above, N):
+            N[0] = int(impl.signal_size(p, bits if bits > 0 else None, above))
+            return GL_OK
 
-    def destroy(self, handle) -> None:
-        handle.close()
+        def footprint(ctx, p, N, out):
+            out[0] = int(impl.footprint(p, N))
+            return GL_OK
 
-    def batch(self, handles: Sequence, high_priority: bool) -> object:
-        return self.gl.Batch(plans=list(handles), high_priority=int(high_priority), **self.opts)
+        def create(ctx, p, N, out):
+            out[0] = put(impl.create(p, N))
+            return GL_OK
 
-    def close_batch(self, batch) -> None:
-        batch.close()
+        def destroy(ctx, h):
+            impl.destroy(self.objs.pop(h))
 
-    def start(self, batch, iters: int) -> None:
-        batch.enqueue(iters)
+        def batch(ctx, tests, n, high, out):
+            out[0] = put(impl.batch([self.objs[tests[i]] for i in range(n)], bool(high)))
+            return GL_OK
 
-    def ready(self, batch) -> bool:
-        return batch.query()
+        def close_batch(ctx, h):
+            impl.close_batch(self.objs.pop(h))
 
-    def finish(self, batch) -> list[tuple[float, int]]:
-        """Per test (max round-off so far in this batch, status) after the enqueued work."""
-        batch.sync_status(check=False)
-        return [batch.test_status(i) for i in range(batch.ntests)]
+        def start(ctx, h, k):
+            impl.start(self.objs[h], int(k))
+            return GL_OK
 
-    def res64(self, handle) -> tuple[int, bool]:
-        return handle.res64_zero()
+        def ready(ctx, h):
+            return 1 if impl.ready(self.objs[h]) else 0
 
+        def finish(ctx, h, n, err, st):
+            res = impl.finish(self.objs[h])
+            for i in range(n):
+                err[i], st[i] = float(res[i][0]), int(res[i][1])
+            return GL_OK
 
-@dataclass
-class _Lane:
-    name: str
-    high: bool
-    live: list = field(default_factory=list)
-    batch: object = None
-    members: tuple = ()
-    iter_ms: float | None = None     # measured ms per iteration of the current members
-    inflight: int = 0                # iterations enqueued and not yet collected
-    t_start: float = 0.0
-    busy_s: float = 0.0
-    steps: int = 0
-    rebuilds: int = 0
-    peak_live: int = 0
+        def res64(ctx, h, r, z):
+            a, b = impl.res64(self.objs[h])
+            r[0], z[0] = int(a), int(bool(b))
+            return GL_OK
+
+        e = gl.ServerEngine()
+        e.ctx = None
+        # the CFUNCTYPE objects must outlive the server: keep them on self
+        self._cbs = [gl.ENGINE_SIGNAL_SIZE(guard(signal_size)), gl.ENGINE_FOOTPRINT(guard(footprint)),
+                     gl.ENGINE_CREATE(guard(create)), gl.ENGINE_DESTROY(guard(destroy, None)),
+                     gl.ENGINE_BATCH(guard(batch)), gl.ENGINE_CLOSE_BATCH(guard(close_batch, None)),
+                     gl.ENGINE_START(guard(start)), gl.ENGINE_READY(guard(ready)), gl.ENGINE_FINISH(guard(finish)),
+                     gl.ENGINE_RES64(guard(res64))]
+        (e.signal_size, e.footprint, e.create, e.destroy, e.batch, e.close_batch, e.start, e.ready, e.finish,
+         e.res64) = self._cbs
+        self.struct = e
 
 
 class Server:
-    def __init__(self, engine, hbm_budget_bytes: float = 150e9, max_active: int = 512, step_ms: float = 50.0,
+    """Options of gl_server_opts; `engine` None runs on the GPU `device`."""
+
+    def __init__(self, engine=None, hbm_budget_bytes: float = 150e9, max_active: int = 512, step_ms: float = 50.0,
                  checkpoint_every: int = 100_000, max_bits_per_word: float | None = None, retries: int = 2,
-                 chain_iterations: int = 100_000, lanes: int = 2, build_threads: int = 2,
-                 clock: Callable[[], float] = time.perf_counter, poll_s: float = 2e-4):
-        """lanes=1 puts every test in one batch (no chain lane)."""
-        self.engine = engine
-        self.budget = int(hbm_budget_bytes)
-        self.max_active = int(max_active)
-        self.step_ms = float(step_ms)
-        self.checkpoint_every = int(checkpoint_every)
-        self.bits = None if max_bits_per_word is None else float(max_bits_per_word)
-        self.retries = int(retries)
-        self.chain_iterations = int(chain_iterations)
-        self.nlanes = 2 if lanes >= 2 else 1
-        self.build_threads = max(1, int(build_threads))
-        self.clock = clock
-        self.poll_s = float(poll_s)
+                 chain_iterations: int = 100_000, lanes: int = 2, build_threads: int = 2, device: int = 0,
+                 error_limit: float = 0.4, check_every: int = 1000):
+        import gpulucas_gb300 as gl
+        self.gl = gl
+        o = gl.ServerOpts()
+        gl.lib.gl_server_default_opts(ctypes.byref(o))
+        o.device, o.hbm_budget_bytes, o.max_active, o.step_ms = device, float(hbm_budget_bytes), max_active, step_ms
+        o.checkpoint_every, o.retries, o.chain_iterations = checkpoint_every, retries, chain_iterations
+        o.max_bits_per_word = 0.0 if max_bits_per_word is None else float(max_bits_per_word)
+        o.lanes, o.build_threads, o.error_limit, o.check_every = lanes, build_threads, error_limit, check_every
+        self.opts = o
+        self.engine = PyEngine(engine) if engine is not None else None
         self.stats: dict = {}
 
-    def _lane_of(self, req: Request) -> int:
-        if self.nlanes == 1:
-            return 0
-        return 0 if (req.full or req.iterations > self.chain_iterations) else 1
-
-    # ------------------------------------------------------------------------
-    def run(self, requests: Iterable[Request], realtime: bool = True) -> list[Completion]:
-        """Serve `requests`.  With realtime, a request is visible only once the wall
-        clock since the start passes its arrival time; otherwise all are queued at once
-        at time 0.  Returns one Completion per request, in completion order; times are
-        seconds since the start."""
+    def run(self, requests: Iterable[Request], realtime: bool = True, poll_ms: float = 2.0) -> list[Completion]:
+        """Serve `requests`: with realtime, each is submitted when the wall clock since
+        the start reaches its arrival time; otherwise all are submitted at once.
+        Returns one Completion per request in completion order (times in seconds since
+        the server started; arrival_s is the submission time)."""
+        gl = self.gl
         reqs = sorted(requests, key=lambda r: (r.arrival_s, r.rid))
-        if not realtime:
-            reqs = [Request(r.rid, 0.0, r.p, r.iterations, r.full) for r in reqs]
-        eng = self.engine
-        t0 = self.clock()
-
-        def now():
-            return self.clock() - t0
-
-        incoming = deque(reqs)
-        queue: deque[_Live] = deque()
-        building: list[_Live] = []
-        lanes = [_Lane("chain", True), _Lane("bulk", False)] if self.nlanes == 2 else [_Lane("all", False)]
+        by_id = {r.rid: r for r in reqs}
+        h = ctypes.c_void_p()
+        eng = ctypes.byref(self.engine.struct) if self.engine is not None else None
+        gl._check(gl.lib.gl_server_create(ctypes.byref(self.opts), eng, ctypes.byref(h)), "server create")
         out: list[Completion] = []
-        used = 0
-        peak_bytes = 0
-        flop_done = 0.0
-        pool = ThreadPoolExecutor(self.build_threads)
-
-        def nlive():
-            return sum(len(ln.live) for ln in lanes)
-
-        def arrive():
-            t = now()
-            while incoming and incoming[0].arrival_s <= t:
-                r = incoming.popleft()
-                N = eng.signal_size(r.p, self.bits)
-                queue.append(_Live(r, N, eng.footprint(r.p, N), 0.0))
-
-        def admit():
-            nonlocal used, peak_bytes
-            while queue and nlive() + len(building) < self.max_active and used + queue[0].nbytes <= self.budget:
-                e = queue.popleft()
-                e.admit_s = now()
-                used += e.nbytes
-                peak_bytes = max(peak_bytes, used)
-                e.future = pool.submit(eng.create, e.req.p, e.N)
-                building.append(e)
-            if queue and not nlive() and not building and queue[0].nbytes > self.budget:
-                e = queue.popleft()   # can never fit: reject rather than wait forever
-                out.append(Completion(e.req.rid, e.req.p, e.N, 0, e.req.full, e.req.arrival_s, now(), now(),
-                                      0, False, False, 0.0, GL_ERR_NOMEM, attempts=e.attempts))
-
-        def collect(block: bool):
-            for e in list(building):
-                if block or e.future.done():
-                    e.handle = e.future.result()
-                    e.future = None
-                    building.remove(e)
-                    lanes[self._lane_of(e.req)].live.append(e)
-                    block = False
-
-        def retire(ln: _Lane, e: _Live, status: int):
-            nonlocal used
-            res, zero = eng.res64(e.handle) if status == GL_OK else (0, False)
-            full_done = e.req.full and e.done == e.req.p - 2
-            eng.destroy(e.handle)
-            used -= e.nbytes
-            if status == GL_ERR_ROUNDOFF and e.attempts <= self.retries:
-                # start again from S0 = 4 at the next larger length, ahead of the queue
-                N = eng.signal_size(e.req.p, self.bits, above=e.N)
-                queue.appendleft(_Live(e.req, N, eng.footprint(e.req.p, N), 0.0, attempts=e.attempts + 1))
-                return
-            out.append(Completion(e.req.rid, e.req.p, e.N, e.done, e.req.full, e.req.arrival_s, e.admit_s, now(),
-                                  res, zero, bool(full_done and zero and status == GL_OK), e.maxerr, status,
-                                  e.checkpoints, e.attempts, ln.name))
-
-        def land(ln: _Lane):
-            """Collect a finished step of lane `ln`: statuses, checkpoints, retirements."""
-            nonlocal flop_done
-            k = ln.inflight
-            st = eng.finish(ln.batch)
-            dt = self.clock() - ln.t_start
-            ln.busy_s += dt
-            ln.iter_ms = dt * 1e3 / k
-            ln.inflight = 0
-            done_now = []
-            for e, (err, s) in zip(ln.live, st):
-                e.done += k
-                e.maxerr = max(e.maxerr, err)
-                flop_done += flop_alg(e.N) * k
-                if s != GL_OK:
-                    done_now.append((e, s))
-                elif e.done >= e.req.iterations:
-                    done_now.append((e, GL_OK))
-                elif e.req.full and self.checkpoint_every > 0 and e.done % self.checkpoint_every == 0:
-                    e.checkpoints.append((e.done, eng.res64(e.handle)[0]))
-            if done_now:
-                eng.close_batch(ln.batch)
-                ln.batch, ln.members = None, ()
-                for e, s in done_now:
-                    ln.live.remove(e)
-                    retire(ln, e, s)
-
-        def launch(ln: _Lane):
-            key = tuple(id(e) for e in ln.live)
-            if key != ln.members:
-                if ln.batch is not None:
-                    eng.close_batch(ln.batch)
-                ln.batch = eng.batch([e.handle for e in ln.live], ln.high)
-                ln.members = key
-                ln.iter_ms = None
-                ln.rebuilds += 1
-            ln.peak_live = max(ln.peak_live, len(ln.live))
-            # bounded by the time budget, the next completion and the next checkpoint
-            k = min(e.req.iterations - e.done for e in ln.live)
-            for e in ln.live:
-                if e.req.full and self.checkpoint_every > 0:
-                    k = min(k, self.checkpoint_every - e.done % self.checkpoint_every)
-            k = min(k, max(1, int(self.step_ms / ln.iter_ms)) if ln.iter_ms else 8)
-            ln.t_start = self.clock()
-            eng.start(ln.batch, k)
-            ln.inflight = k
-            ln.steps += 1
-
+        buf = (gl.Completion * 64)()
+        n = ctypes.c_int()
+        err = GL_OK
         try:
-            while True:
-                arrive()
-                admit()
-                busy = any(ln.inflight for ln in lanes)
-                collect(block=not nlive() and bool(building) and not busy)
-                if not nlive() and not busy:
-                    if not incoming and not queue and not building:
-                        break
-                    if incoming and not queue and not building:
-                        time.sleep(max(0.0, min(0.05, incoming[0].arrival_s - now())))
-                    continue
-                progressed = False
-                for ln in lanes:
-                    if ln.inflight and eng.ready(ln.batch):
-                        land(ln)
-                        progressed = True
-                    if ln.live and not ln.inflight:
-                        launch(ln)
-                        progressed = True
-                if not progressed:
-                    time.sleep(self.poll_s)
+            t0 = time.perf_counter()
+            i = 0
+            while len(out) < len(reqs):
+                now = time.perf_counter() - t0
+                while i < len(reqs) and (not realtime or reqs[i].arrival_s <= now):
+                    r = reqs[i]
+                    gl._check(gl.lib.gl_server_submit(h, r.rid, r.p, 0 if r.full else r.iterations), "submit")
+                    i += 1
+                wait = poll_ms
+                if i < len(reqs) and realtime:
+                    wait = max(0.0, min(poll_ms, (reqs[i].arrival_s - (time.perf_counter() - t0)) * 1e3))
+                err = gl.lib.gl_server_poll(h, buf, 64, ctypes.byref(n), float(wait))
+                if err != GL_OK:
+                    break
+                for c in buf[: n.value]:
+                    out.append(self._completion(h, c, by_id))
+            st = gl.ServerStats()
+            gl.lib.gl_server_get_stats(h, ctypes.byref(st))
+            self.stats = dict(wall_s=st.wall_s, busy_s=max(st.lane_busy_s[0], st.lane_busy_s[1]),
+                              lanes={"chain": dict(busy_s=st.lane_busy_s[0], steps=st.steps[0],
+                                                   rebuilds=st.rebuilds[0], peak_live=st.peak_live[0]),
+                                     "bulk": dict(busy_s=st.lane_busy_s[1], steps=st.steps[1],
+                                                  rebuilds=st.rebuilds[1], peak_live=st.peak_live[1])},
+                              steps=st.steps[0] + st.steps[1], rebuilds=st.rebuilds[0] + st.rebuilds[1],
+                              peak_live=max(st.peak_live[0], st.peak_live[1]), peak_bytes=st.peak_bytes,
+                              flop=st.flop_alg)
         finally:
-            # normal exit leaves nothing live; after an error, free what is left
-            for ln in lanes:
-                if ln.batch is not None:
-                    if ln.inflight:
-                        eng.finish(ln.batch)
-                    eng.close_batch(ln.batch)
-            pool.shutdown(wait=True)
-            for e in building:
-                if e.future is not None and e.future.exception() is None:
-                    eng.destroy(e.future.result())
-            for ln in lanes:
-                for e in ln.live:
-                    eng.destroy(e.handle)
-        wall = now()
-        self.stats = dict(wall_s=wall, busy_s=max(ln.busy_s for ln in lanes),
-                          lanes={ln.name: dict(busy_s=ln.busy_s, steps=ln.steps, rebuilds=ln.rebuilds,
-                                               peak_live=ln.peak_live) for ln in lanes},
-                          steps=sum(ln.steps for ln in lanes), rebuilds=sum(ln.rebuilds for ln in lanes),
-                          peak_live=max(ln.peak_live for ln in lanes), peak_bytes=peak_bytes, flop=flop_done)
+            rc = gl.lib.gl_server_destroy(h)
+        if self.engine is not None and self.engine.error is not None:
+            raise self.engine.error
+        gl._check(err if err != GL_OK else rc, "server")
         return out
+
+    def _completion(self, h, c, by_id) -> Completion:
+        gl = self.gl
+        cps = []
+        if c.n_checkpoints:
+            its = (ctypes.c_int64 * c.n_checkpoints)()
+            res = (ctypes.c_uint64 * c.n_checkpoints)()
+            k = ctypes.c_int()
+            gl._check(gl.lib.gl_server_checkpoints(h, c.id, its, res, c.n_checkpoints, ctypes.byref(k)),
+                      "checkpoints")
+            cps = [(int(its[j]), int(res[j])) for j in range(k.value)]
+        lane = ("chain" if c.lane == 0 else "bulk") if self.opts.lanes >= 2 else "all"
+        return Completion(int(c.id), int(c.p), int(c.N), int(c.iterations), bool(c.full), float(c.arrival_s),
+                          float(c.admit_s), float(c.done_s), int(c.res64), bool(c.is_zero), bool(c.is_prime),
+                          float(c.max_roundoff), int(c.status), cps, int(c.attempts), lane)
 
 
 # ----------------------------------------------------------------------------

@@ -228,6 +228,99 @@ int gl_batch_test_status(const gl_batch* batch, int index, double* max_roundoff,
 int gl_batch_get_info(const gl_batch* batch, gl_batch_info* info);
 int gl_batch_test_info(const gl_batch* batch, int index, gl_plan_info* info);
 
+/* --- serving: a request loop with continuous batching -------------------- */
+
+/* No counterpart in the reference (one test per process, gpuLucas.cu:374-639).  A
+ * server owns a background thread that admits submitted requests against an HBM budget
+ * and a slot limit (arrival order), builds each test's plan on worker threads, and
+ * advances the live tests in two batches on two streams: the chain lane (the device's
+ * highest stream priority) for full tests and requests of more than chain_iterations,
+ * the bulk lane for the rest.  A lane's batch is rebuilt from the live plans when its
+ * membership changes; each step is bounded by step_ms of GPU time and by the next
+ * completion or Res64 checkpoint.  A test whose round-off reaches error_limit restarts
+ * from S0 = 4 at the next larger length (at most `retries` times), as the reference
+ * aborts such a run (gpuLucas.cu:1470-1479).  Residues stay on the device; finished
+ * tests report Res64 / zero test and free their memory. */
+typedef struct gl_server gl_server;
+
+typedef struct gl_server_opts {
+    int device;
+    double hbm_budget_bytes;     /* device bytes the live tests may hold */
+    int max_active;              /* live tests at most */
+    double step_ms;              /* GPU time per lane step at most */
+    int64_t checkpoint_every;    /* Res64 of full tests every this many iterations (0: never) */
+    double max_bits_per_word;    /* > 0: smallest length with p/N <= this; else gl_safe_signal_size */
+    int retries;                 /* restarts at a larger length after a round-off abort */
+    int64_t chain_iterations;    /* requests longer than this go to the chain lane */
+    int lanes;                   /* 2: chain + bulk lanes; 1: one batch */
+    int build_threads;           /* host threads building plans */
+    double error_limit;          /* round-off limit (0, 0.5] */
+    int check_every;             /* round-off read-back interval inside a step */
+    int reserved[8];
+} gl_server_opts;
+
+typedef struct gl_completion {
+    int64_t id;
+    int p, N;
+    int64_t iterations;          /* iterations done (p - 2 for a full test) */
+    int full;
+    int status;                  /* GL_OK, GL_ERR_ROUNDOFF, GL_ERR_NOMEM (never fits), ... */
+    int is_zero, is_prime;
+    uint64_t res64;
+    double max_roundoff;
+    double arrival_s, admit_s, done_s;   /* seconds since gl_server_create */
+    int attempts;                /* 1 + restarts at a larger length */
+    int lane;                    /* 0 chain, 1 bulk (0 with one lane) */
+    int n_checkpoints;           /* Res64 checkpoints recorded (gl_server_checkpoints) */
+    int reserved;
+} gl_completion;
+
+typedef struct gl_server_stats {
+    double wall_s, lane_busy_s[2];
+    int64_t steps[2], rebuilds[2];
+    int peak_live[2];
+    int live, queued, building;
+    size_t bytes_in_use, peak_bytes;
+    double flop_alg;             /* sum over steps of (5 N log2 N + 4 N) x iterations */
+    int64_t submitted, completed;
+} gl_server_stats;
+
+/* The engine a server drives.  The default is the library's own plans and batches on
+ * opts->device; an explicit engine lets the scheduling be exercised without a GPU.
+ * Handles are opaque to the server.  finish() writes, per test of the batch in the
+ * order given to batch(), the max round-off of that batch so far and a status. */
+typedef struct gl_server_engine {
+    void* ctx;
+    int (*signal_size)(void* ctx, int p, double max_bits_per_word, int above, int* N);
+    int (*footprint)(void* ctx, int p, int N, size_t* bytes);
+    int (*create)(void* ctx, int p, int N, void** test);
+    void (*destroy)(void* ctx, void* test);
+    int (*batch)(void* ctx, void* const* tests, int n, int high_priority, void** batch);
+    void (*close_batch)(void* ctx, void* batch);
+    int (*start)(void* ctx, void* batch, int64_t iters);
+    int (*ready)(void* ctx, void* batch);          /* 1 done, 0 running, < 0 error */
+    int (*finish)(void* ctx, void* batch, int n, double* max_roundoff, int* status);
+    int (*res64)(void* ctx, void* test, uint64_t* res64, int* is_zero);
+} gl_server_engine;
+
+int gl_server_default_opts(gl_server_opts* opts);
+int gl_server_create(const gl_server_opts* opts, const gl_server_engine* engine /* NULL: GPU */,
+                     gl_server** server);
+/* Queue a request; iterations 0 asks for the full p - 2 test.  Thread-safe. */
+int gl_server_submit(gl_server* server, int64_t id, int p, int64_t iterations);
+/* Move up to `max` completions (oldest first) into `out`; *n receives how many.  Waits
+ * up to timeout_ms for the first one (0: no wait).  Thread-safe. */
+int gl_server_poll(gl_server* server, gl_completion* out, int max, int* n, double timeout_ms);
+/* Block until every submitted request has completed. */
+int gl_server_drain(gl_server* server);
+/* Res64 checkpoints (iteration, res64) of a completed request, up to `max`. */
+int gl_server_checkpoints(gl_server* server, int64_t id, int64_t* iterations, uint64_t* res64, int max,
+                          int* n);
+int gl_server_get_stats(gl_server* server, gl_server_stats* stats);
+/* Stops the loop (live tests are dropped) and frees everything.  Returns the loop's
+ * first error, if any. */
+int gl_server_destroy(gl_server* server);
+
 /* --- no device allocation ------------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that may not call cudaMalloc (a

@@ -80,3 +80,34 @@ def test_plan_without_gpu_reports_status(gl):
     with pytest.raises(gl.GLError) as ei:
         gl.Plan(44497, 2048)
     assert ei.value.status == gl.GL_ERR_NODEVICE
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the header's structs have the C compiler's sizes and offsets."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    import gpulucas_gb300 as gl
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    pairs = {"gl_plan_opts": gl.PlanOpts, "gl_plan_info": gl.PlanInfo, "gl_iter_report": gl.IterReport,
+             "gl_result": gl.Result, "gl_batch_info": gl.BatchInfo, "gl_server_opts": gl.ServerOpts,
+             "gl_completion": gl.Completion, "gl_server_stats": gl.ServerStats, "gl_server_engine": gl.ServerEngine}
+    inc = os.path.join(ROOT, "include")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gpulucas.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    for cname, py in pairs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)

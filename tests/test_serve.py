@@ -1,6 +1,6 @@
 """Serving loop: continuous batching against an HBM budget.
 
-CPU tests drive the scheduler with an exact integer engine (the NTT oracle) in place of
+CPU tests drive the scheduler with an exact integer engine (Python integers) in place of
 the GPU: admission under the budget and the slot limit, exact stopping at each request's
 iteration count, Res64 checkpoints of full tests, round-off retirement, rejection of a
 request that can never fit.  GPU tests serve a mixed window through the library and
@@ -12,12 +12,38 @@ from gpulucas_gb300 import serve
 from gpulucas_gb300.workloads import Request
 
 
+class IntLL:
+    """S_k mod 2^p - 1 with Python integers (the exact restatement, S_0 = 4)."""
+
+    def __init__(self, p):
+        self.p, self.M, self.s, self.iters_done = p, (1 << p) - 1, 4, 0
+
+    def iterate(self, k):
+        s, M, p = self.s, self.M, self.p
+        for _ in range(k):
+            s = s * s - 2 + M          # >= 0
+            s = (s & M) + (s >> p)     # 2^p == 1
+            s = (s & M) + (s >> p)
+            if s >= M:
+                s -= M
+        self.s = s
+        self.iters_done += k
+        return self
+
+    def res64(self):
+        return self.s & 0xFFFFFFFFFFFFFFFF
+
+    def is_zero(self):
+        return self.s == 0
+
+    def close(self):
+        pass
+
+
 class ExactEngine:
-    """Engine interface over the exact oracle: a 'batch' is the list of live tests."""
+    """Engine interface over exact integer LL: a 'batch' is the list of live tests."""
 
     def __init__(self, bad=(), bytes_per_word=63):
-        import oracle
-        self.oracle = oracle
         self.bad = set(bad)
         self.bpw = bytes_per_word
         self.live_counts = []
@@ -32,7 +58,7 @@ class ExactEngine:
         return self.bpw * N
 
     def create(self, p, N):
-        return self.oracle.Exact(p)
+        return IntLL(p)
 
     def destroy(self, h):
         h.close()
@@ -63,8 +89,7 @@ class ExactEngine:
 
 
 def _exact(p, k):
-    import oracle
-    return oracle.Exact(p).iterate(k).res64()
+    return IntLL(p).iterate(k).res64()
 
 
 def test_serve_exact_results_and_budget():
@@ -90,8 +115,7 @@ def test_serve_exact_results_and_budget():
         if r.full:
             assert c.is_prime and c.res64 == 0          # M4423 and M9941 are prime
             assert [i for i, _ in c.checkpoints] == list(range(1000, r.iterations, 1000))
-            import oracle
-            ex = oracle.Exact(r.p)
+            ex = IntLL(r.p)
             for i, res in c.checkpoints:
                 assert res == ex.iterate(i - ex.iters_done).res64()
         else:
@@ -138,7 +162,7 @@ def test_serve_retry_at_larger_length_recovers():
 
 def test_serve_realtime_arrivals_overlap():
     """Requests arriving while others run join the live set (continuous batching)."""
-    reqs = [Request(i, 0.01 * i, p, 1500, False) for i, p in enumerate([21701, 23209, 44497, 86243])]
+    reqs = [Request(i, 0.01 * i, p, 1500, False) for i, p in enumerate([4423, 9689, 9941, 11213])]
     eng = ExactEngine()
     srv = serve.Server(eng, step_ms=5.0)
     done = srv.run(reqs, realtime=True)
@@ -169,8 +193,7 @@ def test_serve_gpu_each_result_same_alone_and_in_mix(gl, orc):
             Request(4, 0.04, 9689, 9687, True), Request(5, 0.05, 2976221, 200, False),
             Request(6, 0.06, 300007, 1000, False), Request(7, 0.07, 11213, 11211, True),
             Request(8, 0.08, 150001, 500, False), Request(9, 0.09, 44497, 2000, False)]
-    eng = serve.GpuEngine(device=0)
-    srv = serve.Server(eng, hbm_budget_bytes=8e9, checkpoint_every=2000, step_ms=20.0)
+    srv = serve.Server(device=0, hbm_budget_bytes=8e9, checkpoint_every=2000, step_ms=20.0)
     done = srv.run(reqs, realtime=True)
     assert sorted(c.rid for c in done) == list(range(len(reqs)))
     assert srv.stats["peak_live"] >= 3
