@@ -43,7 +43,8 @@ class PlanOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("device", ctypes.c_int), ("error_limit", ctypes.c_double),
                 ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
                 ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("batch_layout", ctypes.c_int),
-                ("high_priority", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("high_priority", ctypes.c_int), ("max_radix_col", ctypes.c_int),
+                ("max_radix_row", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class PlanInfo(ctypes.Structure):

@@ -39,8 +39,8 @@ int dev_alloc(gl_plan* pl, T** ptr, size_t count) {
   return GL_OK;
 }
 
-bool fill_line_plan(int L, LinePlan* lp) {
-  std::vector<int> r = radix_plan(L, kMaxRadix);
+bool fill_line_plan(int L, LinePlan* lp, int max_radix = kMaxRadix) {
+  std::vector<int> r = radix_plan(L, max_radix);
   if (r.empty() || r.size() > 8) return false;
   lp->L = L;
   lp->nst = (int)r.size();
@@ -113,7 +113,11 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
   return out;
 }
 
-int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
+// Layout for M: column length `force_h` (0: the model's best) with line plans whose
+// largest radix is rc (columns) / rr (rows); each line gets one thread per butterfly
+// of its largest-radix stage.
+int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix) {
+  if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
   int bestH = 0;
   for (const auto& c : ranked_layouts(M, sms))
     if (!force_h || c.second == force_h) {
@@ -124,18 +128,19 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g) {
   g->H = bestH;
   g->W = M / bestH;
   g->G = 1;
-  fill_line_plan(g->W, &g->pw);
-  fill_line_plan(g->H, &g->ph);
+  g->rc = rc;
+  g->rr = rr;
+  if (!fill_line_plan(g->W, &g->pw, rr) || !fill_line_plan(g->H, &g->ph, rc)) return GL_ERR_SIZE;
   g->ls_col = padded_stride(g->H);
   g->ls_row = padded_stride(g->W);
   g->sm_col = (size_t)2 * g->ls_col * 16;
   g->sm_row = (size_t)4 * g->ls_row * 16;
-  auto threads = [](int points, int cap) {
-    int t = round_up32((points + kElemsPerThread - 1) / kElemsPerThread);
+  auto threads = [](int points, int per_thread, int cap) {
+    int t = round_up32((points + per_thread - 1) / per_thread);
     return t < 64 ? 64 : (t > cap ? cap : t);
   };
-  g->t_col = threads(g->H, kMaxThreads);
-  g->t_row = threads(2 * g->W, kRowThreads);
+  g->t_col = threads(g->H, rc, kMaxThreads);
+  g->t_row = threads(2 * g->W, rr, kRowThreads);
   return GL_OK;
 }
 
@@ -162,9 +167,9 @@ int stage_offsets(const LinePlan& lp, int* off) {
 
 // Device time of one fused iteration with column length H, measured on zero-filled
 // buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
-double time_layout(int M, int H, int n, int sms, int iters, cudaStream_t s) {
+double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cudaStream_t s) {
   FusedGeom g{};
-  if (choose_fused_geom(M, H, sms, &g) != GL_OK) return -1.0;
+  if (choose_fused_geom(M, H, sms, &g, rc, rr) != GL_OK) return -1.0;
   const int N = 2 * M;
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
@@ -203,34 +208,56 @@ double time_layout(int M, int H, int n, int sms, int iters, cudaStream_t s) {
   return ms;
 }
 
-// Autotuned column length for M on this device: the cheapest few layouts of the cost
-// model are timed and the fastest kept, once per (M, SM count) per process.
+// Autotuned layout for M on this device: the cheapest few column lengths of the cost
+// model are timed and the fastest kept, once per (M, SM count) per process.  Below
+// 2^17 complex points the lines are too short to fill the GPU with one thread per
+// radix-8 butterfly, so the three best lengths are also timed with radix-4 caps (and
+// radix-2 caps below 2^15).
+struct TunedLayout {
+  int H = 0, rc = kMaxRadix, rr = kMaxRadix;
+  double ms = 0.0;
+};
 std::mutex g_tune_mutex;
-std::map<std::pair<int, int>, std::pair<int, double>> g_tune_cache;
+std::map<std::pair<int, int>, TunedLayout> g_tune_cache;
 
-int autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_out) {
+TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_out) {
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find({M, sms});
     if (it != g_tune_cache.end()) {
-      if (ms_out) *ms_out = it->second.second;
-      return it->second.first;
+      if (ms_out) *ms_out = it->second.ms;
+      return it->second;
     }
   }
   const auto ranked = ranked_layouts(M, sms);
-  int best = 0;
+  TunedLayout best;
   double best_ms = 1e300;
   const int iters = M >= (1 << 18) ? 10 : 40;
-  for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
-    const double ms = time_layout(M, ranked[i].second, n, sms, iters, s);
+  auto consider = [&](int H, int rc, int rr) {
+    const double ms = time_layout(M, H, rc, rr, n, sms, iters, s);
     if (ms > 0.0 && ms < best_ms) {
       best_ms = ms;
-      best = ranked[i].second;
+      best.H = H;
+      best.rc = rc;
+      best.rr = rr;
     }
-  }
-  if (!best) return 0;
+  };
+  for (size_t i = 0; i < ranked.size() && i < 6; ++i) consider(ranked[i].second, kMaxRadix, kMaxRadix);
+  if (M < (1 << 17))
+    for (size_t i = 0; i < ranked.size() && i < 3; ++i) {
+      consider(ranked[i].second, 4, kMaxRadix);
+      consider(ranked[i].second, kMaxRadix, 4);
+      consider(ranked[i].second, 4, 4);
+      if (M < (1 << 15)) {  // lines of at most a few hundred points: radix-2 stages too
+        consider(ranked[i].second, 2, 4);
+        consider(ranked[i].second, 4, 2);
+        consider(ranked[i].second, 2, 2);
+      }
+    }
+  if (!best.H) return best;
+  best.ms = best_ms;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
-  g_tune_cache[{M, sms}] = {best, best_ms};
+  g_tune_cache[{M, sms}] = best;
   if (ms_out) *ms_out = best_ms;
   return best;
 }
@@ -405,10 +432,18 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess) return GL_ERR_CUDA;
   if (sms_override > 0) sms = sms_override;
-  int force_h = o.fft_h;
-  if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override)
-    force_h = autotune_layout(M, n, sms, 0, nullptr);
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg) : choose_plain_geom(M, &pg);
+  int force_h = o.fft_h, cap_c = o.max_radix_col ? o.max_radix_col : kMaxRadix,
+      cap_r = o.max_radix_row ? o.max_radix_row : kMaxRadix;
+  if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
+    const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
+    if (t.H) {
+      force_h = t.H;
+      if (!o.max_radix_col) cap_c = t.rc;
+      if (!o.max_radix_row) cap_r = t.rr;
+    }
+  }
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r)
+                                   : choose_plain_geom(M, &pg);
   if (rc != GL_OK) return rc;
 
   gl_plan* pl = new (std::nothrow) gl_plan();
@@ -559,7 +594,9 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device);
   if (sms <= 0) sms = 152;  // GB300
   if (o.batch_layout) sms = 1;
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg)
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg,
+                                                       o.max_radix_col ? o.max_radix_col : kMaxRadix,
+                                                       o.max_radix_row ? o.max_radix_row : kMaxRadix)
                                    : choose_plain_geom(tmp.M, &tmp.pg);
   if (rc != GL_OK) return rc;
   tmp.device = -1;

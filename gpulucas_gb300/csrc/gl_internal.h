@@ -46,6 +46,9 @@ constexpr unsigned kStatusSlice = 2u;  // product bits beyond what n+1 slices pl
 // is stored column-major: word j = 2(m1 + W m2) + e lives at 2(m1 H + m2) + e.
 struct FusedGeom {
   int W, H, G;
+  int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
+                             // a smaller cap means more, shorter butterflies per stage and
+                             // so more threads per line, for lengths too short to fill the GPU
   int ls_col, ls_row;        // padded shared-memory line strides (complex)
   int t_col, t_row;          // threads per CTA
   size_t sm_col, sm_row;     // dynamic shared memory bytes

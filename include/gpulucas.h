@@ -55,7 +55,9 @@ typedef struct {
     int batch_layout;      /* 1: layout for running inside a batch (total work, no timing) */
     int high_priority;     /* 1: the plan's (or batch's) stream gets the device's highest
                               priority, so its blocks are scheduled ahead of other work */
-    int reserved[5];
+    int max_radix_col;     /* fused form: largest radix of the column / row line plans */
+    int max_radix_row;     /* (8, 4 or 2; 0 = 8, or the autotuner's choice) */
+    int reserved[3];
 } gl_plan_opts;
 
 typedef struct {

@@ -91,6 +91,19 @@ def test_device_residue_matches_oracle(gl, orc, p, N, mode):
             assert pl.res64_zero() == (r, z)
 
 
+@pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432), (2976221, 163840)])
+@pytest.mark.parametrize("caps", [(4, 4), (2, 2), (4, 8), (8, 2)])
+def test_radix_capped_layouts_match_oracle(gl, orc, p, N, caps):
+    """Line plans with smaller radices (more threads per line, for short lengths) give
+    the same integer products as the oracle."""
+    with gl.Plan(p, N, max_radix_col=caps[0], max_radix_row=caps[1], autotune=0) as pl:
+        assert max(pl.info.radix_h) <= max(caps[0], 7) and max(pl.info.radix_w) <= max(caps[1], 7)
+        o = orc.IBDWT(p, N)
+        pl.iterate(9)
+        o.iterate(9)
+        assert (pl.products() == o.ll()).all()
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432)])
 def test_dice_through_abi(gl, orc, p, N):
     """llintToBalInt<n> semantics on arbitrary products via gl_set_products."""
