@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgpulucas_gb300.so")
 HOSTCHECK = os.path.join(HERE, "libgl_hostcheck.so")
+CLI = os.path.join(HERE, "gpulucas")
 
 SOURCES = ["gl_kernels.cu", "gl_residue.cu", "gl_capi.cpp", "gl_tables.cpp", "gl_noalloc.cu", "gl_checkpoint.cpp", "gl_server.cpp",
            "gl_batch.cpp"]
@@ -79,7 +80,20 @@ def build(verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The `gpulucas` executable (the reference's command line) linked to the library."""
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(HERE, "..", "include"),
+           os.path.join(CSRC, "gl_cli.cpp"), "-o", tmp, "-L", HERE, "-lgpulucas_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def build_hostcheck() -> str:

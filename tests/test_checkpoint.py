@@ -124,3 +124,46 @@ def test_cli_checkpoint_resume_and_result_line(tmp_path):
     assert "Resuming" in r2.stdout
     assert (tmp_path / "results.txt").read_text().strip() == f"M( {p} )P, n = {N}, gpulucas_gb300"
     assert not os.path.exists(tmp_path / f"{p}.chk")
+
+
+CLI_BIN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpulucas_gb300", "gpulucas")
+
+
+def test_native_cli_usage_and_errors(tmp_path):
+    """The C++ `gpulucas` executable: usage, argument errors, and a loud failure (no CPU
+    path) when no GPU is usable."""
+    import subprocess
+    if not os.path.exists(CLI_BIN):
+        pytest.skip("gpulucas executable not built")
+    r = subprocess.run([CLI_BIN, "-h"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage: gpulucas" in r.stderr
+    r = subprocess.run([CLI_BIN, "-f", "2048"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "testPrime not specified" in r.stderr
+    r = subprocess.run([CLI_BIN, "-m", "fast", "44497"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+    r = subprocess.run([CLI_BIN, "-d", "99", "-k", "10", "-f", "2048", "44497"], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 3 and not os.path.exists(tmp_path / "results.txt")
+
+
+@pytest.mark.gpu
+def test_native_cli_res64_checkpoint_and_result_line(tmp_path):
+    """The C++ executable: Res64 after k iterations equals the golden value; -c writes
+    <p>.chk in the reference's format, a second run resumes, a full test appends the
+    result line and removes the checkpoint files."""
+    import subprocess
+    r = subprocess.run([CLI_BIN, "-k", "1000", "-f", "2048", "44497"], cwd=tmp_path, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Iter 1000: 0xd76d70f8f0325ccb" in r.stdout
+    p, N = 4423, 256
+    r1 = subprocess.run([CLI_BIN, "-f", str(N), "-c", "1000", "-k", "2000", str(p)], cwd=tmp_path,
+                        capture_output=True, text=True, timeout=300)
+    assert r1.returncode == 0, r1.stderr
+    assert os.path.exists(tmp_path / f"{p}.chk")
+    r2 = subprocess.run([CLI_BIN, "-c", "1000", "-m", "plain", str(p)], cwd=tmp_path, capture_output=True, text=True,
+                        timeout=300)
+    assert r2.returncode == 0, r2.stderr
+    assert "Resuming" in r2.stdout
+    assert (tmp_path / "results.txt").read_text().strip() == f"M( {p} )P, n = {N}, gpulucas_gb300"
+    assert not os.path.exists(tmp_path / f"{p}.chk")
