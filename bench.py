@@ -35,6 +35,7 @@ P3, N3 = 43112609, 2359296
 BY_LENGTH = [("c1", 44497, 2048), ("c2", 2976221, 163840), ("c3", P3, N3)]
 REF_PUBLISHED_ITER_S = 204.72  # gpuLucas.cu:92-96, p=42643801 at N=2359296 (GTX 480 / C2050)
 L2_FLUSH_BYTES = 512 << 20
+WORKLOAD = f"single LL test, one iteration per step of p={P3} at N={N3} (2^18*3^2)"
 
 
 def flop_alg(N: int) -> float:
@@ -190,9 +191,9 @@ def run_reference(args, world: int, rank: int):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: the LL sequence from S0=4 (no dataset)",
-        "config": {"workload": f"LL iteration of p={P3} at N={N3} (2^18*3^2), CPU IBDWT restatement of "
-                               "the reference path (oracle/ibdwt_oracle.c), all host threads",
-                   "p": P3, "N": N3},
+        "config": {"workload": WORKLOAD, "p": P3, "N": N3,
+                   "implementation": "CPU IBDWT restatement of the reference path (oracle/ibdwt_oracle.c), "
+                                     "all host threads"},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} timed iterations after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -290,7 +291,7 @@ def run_ours(args, world: int, rank: int, local: int):
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / REF_PUBLISHED_ITER_S / world, "dtype": "f64",
         "data": "synthetic: the LL sequence from S0=4 (no dataset)",
-        "config": {"workload": f"fused single LL test, one iteration of p={P3} at N={N3} (2^18*3^2)",
+        "config": {"workload": WORKLOAD,
                    "p": P3, "N": N3, "fft": f"{info.fft_h} x {info.fft_w}", "parallelism": "replicas",
                    "l2": "flushed before every timed step (512 MiB write); working set ~110 MB < L2",
                    "vs_baseline_note": "reference's published 204.72 iter/s at N=2359296 (GTX 480/C2050)"},
