@@ -79,8 +79,8 @@ class Completion(ctypes.Structure):
 
 
 class ServerStats(ctypes.Structure):
-    _fields_ = [("wall_s", ctypes.c_double), ("lane_busy_s", ctypes.c_double * 2), ("steps", ctypes.c_int64 * 2),
-                ("rebuilds", ctypes.c_int64 * 2), ("peak_live", ctypes.c_int * 2), ("live", ctypes.c_int),
+    _fields_ = [("wall_s", ctypes.c_double), ("lane_busy_s", ctypes.c_double * 3), ("steps", ctypes.c_int64 * 3),
+                ("rebuilds", ctypes.c_int64 * 3), ("peak_live", ctypes.c_int * 3), ("live", ctypes.c_int),
                 ("queued", ctypes.c_int), ("building", ctypes.c_int), ("bytes_in_use", ctypes.c_size_t),
                 ("peak_bytes", ctypes.c_size_t), ("flop_alg", ctypes.c_double), ("submitted", ctypes.c_int64),
                 ("completed", ctypes.c_int64)]

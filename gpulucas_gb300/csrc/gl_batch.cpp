@@ -233,7 +233,7 @@ int gl_batch_create(const int* p, const int* N, int ntests, const gl_plan_opts* 
     delete b;
     return GL_ERR_NODEVICE;
   }
-  GB_TRY(gl_make_stream(&b->stream, o.high_priority != 0) == cudaSuccess ? GL_OK : GL_ERR_CUDA);
+  GB_TRY(gl_make_stream(&b->stream, o.high_priority) == cudaSuccess ? GL_OK : GL_ERR_CUDA);
   for (int i = 0; i < ntests; ++i) {
     int n_i = N ? N[i] : 0;
     if (n_i == 0) GB_TRY(gl_smallest_signal_size(p[i], 19.5, &n_i));
@@ -266,7 +266,7 @@ int gl_batch_create_from_plans(gl_plan* const* plans, int nplans, const gl_plan_
   b->check_every = o.check_every;
   b->error_limit = o.error_limit;
   if (cudaSetDevice(b->device) != cudaSuccess ||
-      gl_make_stream(&b->stream, o.high_priority != 0) != cudaSuccess) {
+      gl_make_stream(&b->stream, o.high_priority) != cudaSuccess) {
     free_batch(b);
     return GL_ERR_CUDA;
   }

@@ -84,6 +84,16 @@ double line_ops(const LinePlan& lp) {
 
 int padded_stride(int L) { return L + (L >> 4) + 1; }
 
+// Radix caps of a layout chosen without timing: below 2^17 complex points a single test
+// cannot fill the device with one thread per radix-8 butterfly, and the timed search
+// picks radix-4 caps there (more warps per line); a batch member keeps radix 8 (the batch
+// fills the device).  Explicit options win.
+void model_caps(int M, const gl_plan_opts& o, int sms_override, int* rc, int* rr) {
+  const bool small = M < (1 << 17) && !sms_override && !o.fft_h;
+  *rc = o.max_radix_col ? o.max_radix_col : (small ? 4 : kMaxRadix);
+  *rr = o.max_radix_row ? o.max_radix_row : (small ? 4 : kMaxRadix);
+}
+
 // Pick M = W * H for `sms` SMs.  Work units: W columns (column passes, one per CTA)
 // and H/2+1 row pairs (row pass).  With equal units per kernel the busiest SM runs
 // ceil(units / sms) of them, so the modelled time is the sum over the three kernels
@@ -386,13 +396,14 @@ int gl_plan_create(int p, int N, const gl_plan_opts* opts, gl_plan** out) {
 
 }  // extern "C"
 
-cudaError_t gl_make_stream(cudaStream_t* s, bool high) {
+cudaError_t gl_make_stream(cudaStream_t* s, int level) {
   int least = 0, greatest = 0;
-  if (high) {
+  if (level) {
     const cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e != cudaSuccess) return e;
   }
-  return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, high ? greatest : least);
+  const int prio = level == 1 ? greatest : (level == 2 ? (greatest + least) / 2 : least);
+  return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, prio);
 }
 
 void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters) {
@@ -419,6 +430,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   if (p < 3 || N < 16 || (N & 1) || N > p) return GL_ERR_ARG;
   if (o.mode != GL_MODE_FUSED && o.mode != GL_MODE_PLAIN) return GL_ERR_ARG;
   if (!(o.error_limit > 0.0 && o.error_limit <= 0.5) || o.check_every < 1) return GL_ERR_ARG;
+  if (o.high_priority < 0 || o.high_priority > 2) return GL_ERR_ARG;
   const int n = slice_depth(p, N);
   if (n < 0) return GL_ERR_RATIO;
   const int M = N / 2;
@@ -432,8 +444,8 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess) return GL_ERR_CUDA;
   if (sms_override > 0) sms = sms_override;
-  int force_h = o.fft_h, cap_c = o.max_radix_col ? o.max_radix_col : kMaxRadix,
-      cap_r = o.max_radix_row ? o.max_radix_row : kMaxRadix;
+  int force_h = o.fft_h, cap_c = kMaxRadix, cap_r = kMaxRadix;
+  model_caps(M, o, sms_override, &cap_c, &cap_r);
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
@@ -463,7 +475,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   } while (0)
 #define GL_TRYC(x) GL_TRY(cuda_status(x))
 
-  GL_TRYC(gl_make_stream(&pl->stream, o.high_priority != 0));
+  GL_TRYC(gl_make_stream(&pl->stream, o.high_priority));
   GL_TRYC(cudaEventCreate(&pl->ev0));
   GL_TRYC(cudaEventCreate(&pl->ev1));
   GL_TRYC(cudaMallocHost((void**)&pl->h_status, sizeof(Status)));
@@ -594,9 +606,9 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device);
   if (sms <= 0) sms = 152;  // GB300
   if (o.batch_layout) sms = 1;
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg,
-                                                       o.max_radix_col ? o.max_radix_col : kMaxRadix,
-                                                       o.max_radix_row ? o.max_radix_row : kMaxRadix)
+  int cap_c = kMaxRadix, cap_r = kMaxRadix;
+  model_caps(tmp.M, o, o.batch_layout ? 1 : 0, &cap_c, &cap_r);
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(tmp.M, o.fft_h, sms, &tmp.fg, cap_c, cap_r)
                                    : choose_plain_geom(tmp.M, &tmp.pg);
   if (rc != GL_OK) return rc;
   tmp.device = -1;

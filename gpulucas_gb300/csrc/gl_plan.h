@@ -40,7 +40,7 @@ struct gl_plan {
 int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, gl_plan** out);
 // iterations done outside the plan's own launches (by a batch): bookkeeping only
 void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters);
-// non-blocking stream, at the device's highest priority when `high` is set
-cudaError_t gl_make_stream(cudaStream_t* s, bool high);
+// non-blocking stream; level 0: normal priority, 1: the device's highest, 2: between
+cudaError_t gl_make_stream(cudaStream_t* s, int level);
 // cost of one column-pass unit and one row-pass unit of a fused plan (FP64 model)
 double gl_plan_unit_cost(const gl_plan* pl, bool row);

@@ -7,7 +7,9 @@
 //      allow, handing each to the builders (a request that can never fit is rejected
 //      once nothing else is live);
 //   3. moves built tests into their lane (chain: full tests and long requests; bulk:
-//      the rest);
+//      the rest) and keeps the chain test with the most iterations left alone in the
+//      lead lane (highest stream priority), so the longest dependent chain runs at its
+//      own speed while everything else fills the rest of the device;
 //   4. for each lane: if its step has finished, reads every test's round-off and status,
 //      records checkpoints, retires finished or failed tests (a round-off failure
 //      re-queues the request at the next larger length while retries remain) and drops
@@ -15,7 +17,7 @@
 //      rebuilds the batch when needed and enqueues the next step: at most step_ms of
 //      GPU time (from the last measured step), never past the next completion or
 //      checkpoint of its tests.
-// Steps are enqueued asynchronously and polled, so both lanes' streams stay busy while
+// Steps are enqueued asynchronously and polled, so the lanes' streams stay busy while
 // the host sizes, admits and retires.
 #include <algorithm>
 #include <chrono>
@@ -124,7 +126,7 @@ struct Live {
 };
 
 struct Lane {
-  bool high = false;
+  int level = 0;          // stream priority level (gl_plan_opts.high_priority)
   std::vector<Live*> live;
   void* batch = nullptr;
   std::vector<Live*> members;
@@ -159,8 +161,8 @@ struct gl_server {
   // loop state (loop thread only)
   std::deque<Live*> queue;
   int building = 0;
-  Lane lanes[2];
-  int nlanes = 2;
+  Lane lanes[3];
+  int nlanes = 3;
   size_t used = 0;
 
   std::thread loop_thread;
@@ -171,9 +173,42 @@ struct gl_server {
 
 namespace {
 
+// Lanes: with three, 0 = lead (the chain test with the most iterations left, alone, at
+// the highest priority), 1 = chain (the other long tests), 2 = bulk; with two, 0 = chain,
+// 1 = bulk; with one, everything in lane 0.
 int lane_of(const gl_server* s, const Request& r) {
   if (s->nlanes == 1) return 0;
-  return (r.full || r.iterations > s->o.chain_iterations) ? 0 : 1;
+  const bool chain = r.full || r.iterations > s->o.chain_iterations;
+  return chain ? s->nlanes - 2 : s->nlanes - 1;
+}
+
+// Three lanes: keep the chain test with the most iterations left alone in the lead lane.
+// Moves happen only while both lanes are idle; returns true if a move is pending.
+bool promote(gl_server* s) {
+  if (s->nlanes != 3) return false;
+  Lane& L = s->lanes[0];
+  Lane& C = s->lanes[1];
+  Live* best = nullptr;
+  int64_t best_rem = -1;
+  for (Lane* ln : {&L, &C})
+    for (Live* e : ln->live) {
+      const int64_t rem = e->r.iterations - e->done;
+      if (rem > best_rem) {
+        best_rem = rem;
+        best = e;
+      }
+    }
+  if (!best || (L.live.size() == 1 && L.live[0] == best)) return false;
+  if (!L.live.empty()) {  // hysteresis: the lead runs faster, so counts cross often
+    const int64_t lead_rem = L.live[0]->r.iterations - L.live[0]->done;
+    if (best_rem <= lead_rem + lead_rem / 4) return false;
+  }
+  if (L.inflight || C.inflight) return true;
+  for (Live* e : L.live) C.live.push_back(e);
+  L.live.clear();
+  C.live.erase(std::find(C.live.begin(), C.live.end(), best));
+  L.live.push_back(best);
+  return false;
 }
 
 void complete(gl_server* s, const Live& e, int status, uint64_t res, bool zero, int lane) {
@@ -364,7 +399,7 @@ int launch(gl_server* s, int li) {
     ln.batch = nullptr;
     std::vector<void*> tests;
     for (Live* e : ln.live) tests.push_back(e->test);
-    const int rc = s->eng.batch(s->eng.ctx, tests.data(), (int)tests.size(), ln.high ? 1 : 0, &ln.batch);
+    const int rc = s->eng.batch(s->eng.ctx, tests.data(), (int)tests.size(), ln.level, &ln.batch);
     if (rc != GL_OK) return rc;
     ln.members = ln.live;
     ln.iter_ms = 0.0;
@@ -389,7 +424,7 @@ int launch(gl_server* s, int li) {
 void publish_stats(gl_server* s) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->stats.wall_s = s->now();
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 3; ++i) {
     s->stats.lane_busy_s[i] = s->lanes[i].busy_s;
     s->stats.steps[i] = s->lanes[i].steps;
     s->stats.rebuilds[i] = s->lanes[i].rebuilds;
@@ -437,7 +472,13 @@ void loop_main(gl_server* s) {
           progressed = true;
         }
       }
-      if (rc == GL_OK && !ln.live.empty() && !ln.inflight) {
+    }
+    // a pending move between the lead and chain lanes holds both until they are idle
+    const bool hold = rc == GL_OK && promote(s);
+    for (int i = 0; i < s->nlanes && rc == GL_OK; ++i) {
+      Lane& ln = s->lanes[i];
+      if (hold && i < 2) continue;
+      if (!ln.live.empty() && !ln.inflight) {
         rc = launch(s, i);
         progressed = true;
       }
@@ -487,7 +528,7 @@ int gl_server_default_opts(gl_server_opts* o) {
   o->max_bits_per_word = 0.0;
   o->retries = 2;
   o->chain_iterations = 100000;
-  o->lanes = 2;
+  o->lanes = 3;
   o->build_threads = 2;
   o->error_limit = 0.4;
   o->check_every = 1000;
@@ -506,8 +547,13 @@ int gl_server_create(const gl_server_opts* opts, const gl_server_engine* engine,
     return GL_ERR_ARG;
   gl_server* s = new gl_server();
   s->o = o;
-  s->nlanes = o.lanes >= 2 ? 2 : 1;
-  s->lanes[0].high = s->nlanes == 2;
+  s->nlanes = o.lanes >= 3 ? 3 : (o.lanes == 2 ? 2 : 1);
+  if (s->nlanes == 3) {
+    s->lanes[0].level = 1;  // lead: the device's highest priority
+    s->lanes[1].level = 2;  // chain: between
+  } else if (s->nlanes == 2) {
+    s->lanes[0].level = 1;
+  }
   if (engine) {
     s->eng = *engine;
     if (!s->eng.signal_size || !s->eng.footprint || !s->eng.create || !s->eng.destroy || !s->eng.batch ||

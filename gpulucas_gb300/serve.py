@@ -5,7 +5,9 @@ background thread admits submitted requests against an HBM budget and a slot lim
 builds each test's plan on worker threads, and advances the live tests in two batches on
 two streams -- the chain lane (the device's highest stream priority) for full tests and
 long requests, whose latency is a chain of dependent iterations too small to fill the
-GPU, and the bulk lane for the rest, which soaks up the SMs the chain lane leaves idle.
+GPU, and the bulk lane for the rest, which soaks up the SMs the chain lane leaves idle;
+the chain test with the most iterations left runs alone in a lead lane at the highest
+priority, since the longest dependent chain sets the makespan.
 A lane's batch is rebuilt from the live plans when its membership changes; every step is
 bounded by `step_ms` of GPU time and by the next completion or Res64 checkpoint, so an
 arrival waits at most one step.  A test whose round-off reaches the limit restarts from
@@ -160,7 +162,7 @@ class Server:
 
     def __init__(self, engine=None, hbm_budget_bytes: float = 150e9, max_active: int = 512, step_ms: float = 50.0,
                  checkpoint_every: int = 100_000, max_bits_per_word: float | None = None, retries: int = 2,
-                 chain_iterations: int = 100_000, lanes: int = 2, build_threads: int = 2, device: int = 0,
+                 chain_iterations: int = 100_000, lanes: int = 3, build_threads: int = 2, device: int = 0,
                  error_limit: float = 0.4, check_every: int = 1000):
         import gpulucas_gb300 as gl
         self.gl = gl
@@ -208,13 +210,13 @@ class Server:
                     out.append(self._completion(h, c, by_id))
             st = gl.ServerStats()
             gl.lib.gl_server_get_stats(h, ctypes.byref(st))
-            self.stats = dict(wall_s=st.wall_s, busy_s=max(st.lane_busy_s[0], st.lane_busy_s[1]),
-                              lanes={"chain": dict(busy_s=st.lane_busy_s[0], steps=st.steps[0],
-                                                   rebuilds=st.rebuilds[0], peak_live=st.peak_live[0]),
-                                     "bulk": dict(busy_s=st.lane_busy_s[1], steps=st.steps[1],
-                                                  rebuilds=st.rebuilds[1], peak_live=st.peak_live[1])},
-                              steps=st.steps[0] + st.steps[1], rebuilds=st.rebuilds[0] + st.rebuilds[1],
-                              peak_live=max(st.peak_live[0], st.peak_live[1]), peak_bytes=st.peak_bytes,
+            names = self._lane_names()
+            self.stats = dict(wall_s=st.wall_s, busy_s=max(st.lane_busy_s[i] for i in range(len(names))),
+                              lanes={nm: dict(busy_s=st.lane_busy_s[i], steps=st.steps[i], rebuilds=st.rebuilds[i],
+                                              peak_live=st.peak_live[i]) for i, nm in enumerate(names)},
+                              steps=sum(st.steps[i] for i in range(len(names))),
+                              rebuilds=sum(st.rebuilds[i] for i in range(len(names))),
+                              peak_live=max(st.peak_live[i] for i in range(len(names))), peak_bytes=st.peak_bytes,
                               flop=st.flop_alg)
         finally:
             rc = gl.lib.gl_server_destroy(h)
@@ -222,6 +224,10 @@ class Server:
             raise self.engine.error
         gl._check(err if err != GL_OK else rc, "server")
         return out
+
+    def _lane_names(self):
+        n = self.opts.lanes
+        return ["lead", "chain", "bulk"] if n >= 3 else (["chain", "bulk"] if n == 2 else ["all"])
 
     def _completion(self, h, c, by_id) -> Completion:
         gl = self.gl
@@ -233,7 +239,7 @@ class Server:
             gl._check(gl.lib.gl_server_checkpoints(h, c.id, its, res, c.n_checkpoints, ctypes.byref(k)),
                       "checkpoints")
             cps = [(int(its[j]), int(res[j])) for j in range(k.value)]
-        lane = ("chain" if c.lane == 0 else "bulk") if self.opts.lanes >= 2 else "all"
+        lane = self._lane_names()[c.lane]
         return Completion(int(c.id), int(c.p), int(c.N), int(c.iterations), bool(c.full), float(c.arrival_s),
                           float(c.admit_s), float(c.done_s), int(c.res64), bool(c.is_zero), bool(c.is_prime),
                           float(c.max_roundoff), int(c.status), cps, int(c.attempts), lane)

@@ -53,8 +53,9 @@ typedef struct {
     int cols_per_cta;      /* 0 or 1 (the column passes take one column per CTA) */
     int autotune;          /* 1 (default): time the best few layouts once per N per process */
     int batch_layout;      /* 1: layout for running inside a batch (total work, no timing) */
-    int high_priority;     /* 1: the plan's (or batch's) stream gets the device's highest
-                              priority, so its blocks are scheduled ahead of other work */
+    int high_priority;     /* stream priority of the plan (or batch): 0 normal, 1 the device's
+                              highest, 2 between the two; higher-priority blocks are
+                              scheduled ahead of other work */
     int max_radix_col;     /* fused form: largest radix of the column / row line plans */
     int max_radix_row;     /* (8, 4 or 2; 0 = 8, or the autotuner's choice) */
     int reserved[3];
@@ -235,9 +236,10 @@ int gl_batch_test_info(const gl_batch* batch, int index, gl_plan_info* info);
 /* No counterpart in the reference (one test per process, gpuLucas.cu:374-639).  A
  * server owns a background thread that admits submitted requests against an HBM budget
  * and a slot limit (arrival order), builds each test's plan on worker threads, and
- * advances the live tests in two batches on two streams: the chain lane (the device's
- * highest stream priority) for full tests and requests of more than chain_iterations,
- * the bulk lane for the rest.  A lane's batch is rebuilt from the live plans when its
+ * advances the live tests in batches on separate streams: the lead lane (the device's
+ * highest stream priority) runs alone the long test with the most iterations left, the
+ * chain lane (next priority) the other full tests and requests of more than
+ * chain_iterations, the bulk lane (normal priority) the rest.  A lane's batch is rebuilt from the live plans when its
  * membership changes; each step is bounded by step_ms of GPU time and by the next
  * completion or Res64 checkpoint.  A test whose round-off reaches error_limit restarts
  * from S0 = 4 at the next larger length (at most `retries` times), as the reference
@@ -254,7 +256,7 @@ typedef struct gl_server_opts {
     double max_bits_per_word;    /* > 0: smallest length with p/N <= this; else gl_safe_signal_size */
     int retries;                 /* restarts at a larger length after a round-off abort */
     int64_t chain_iterations;    /* requests longer than this go to the chain lane */
-    int lanes;                   /* 2: chain + bulk lanes; 1: one batch */
+    int lanes;                   /* 3: lead + chain + bulk; 2: chain + bulk; 1: one batch */
     int build_threads;           /* host threads building plans */
     double error_limit;          /* round-off limit (0, 0.5] */
     int check_every;             /* round-off read-back interval inside a step */
@@ -272,15 +274,15 @@ typedef struct gl_completion {
     double max_roundoff;
     double arrival_s, admit_s, done_s;   /* seconds since gl_server_create */
     int attempts;                /* 1 + restarts at a larger length */
-    int lane;                    /* 0 chain, 1 bulk (0 with one lane) */
+    int lane;                    /* 3 lanes: 0 lead, 1 chain, 2 bulk; 2: 0 chain, 1 bulk */
     int n_checkpoints;           /* Res64 checkpoints recorded (gl_server_checkpoints) */
     int reserved;
 } gl_completion;
 
 typedef struct gl_server_stats {
-    double wall_s, lane_busy_s[2];
-    int64_t steps[2], rebuilds[2];
-    int peak_live[2];
+    double wall_s, lane_busy_s[3];
+    int64_t steps[3], rebuilds[3];
+    int peak_live[3];
     int live, queued, building;
     size_t bytes_in_use, peak_bytes;
     double flop_alg;             /* sum over steps of (5 N log2 N + 4 N) x iterations */
@@ -290,7 +292,8 @@ typedef struct gl_server_stats {
 /* The engine a server drives.  The default is the library's own plans and batches on
  * opts->device; an explicit engine lets the scheduling be exercised without a GPU.
  * Handles are opaque to the server.  finish() writes, per test of the batch in the
- * order given to batch(), the max round-off of that batch so far and a status. */
+ * order given to batch(), the max round-off of that batch so far and a status;
+ * batch()'s priority is a gl_plan_opts.high_priority level. */
 typedef struct gl_server_engine {
     void* ctx;
     int (*signal_size)(void* ctx, int p, double max_bits_per_word, int above, int* N);

@@ -105,8 +105,9 @@ def test_serve_exact_results_and_budget():
     done = srv.run(reqs, realtime=False)
     assert sorted(c.rid for c in done) == list(range(len(reqs)))
     assert srv.stats["peak_bytes"] <= budget and max(eng.live_counts) <= 3
-    assert eng.lanes_seen == {True, False}          # full tests ran in the chain lane
-    assert {c.lane for c in done if reqs[c.rid].full} == {"chain"}
+    assert eng.lanes_seen == {True, False}          # full tests ran in the priority lanes
+    assert {c.lane for c in done if reqs[c.rid].full} <= {"lead", "chain"}
+    assert "lead" in {c.lane for c in done}
     assert {c.lane for c in done if not reqs[c.rid].full} == {"bulk"}
     for c in done:
         r = reqs[c.rid]
@@ -222,3 +223,18 @@ def test_describe_predicts_batch_plan_footprint(gl):
             assert pl.info.device_bytes <= est <= 1.05 * pl.info.device_bytes + 4096, (p, N)
             assert (pl.info.fft_h, pl.info.fft_w) == (gl.describe(p, N, batch_layout=1).fft_h,
                                                       gl.describe(p, N, batch_layout=1).fft_w)
+
+
+def test_serve_lead_lane_holds_longest_chain():
+    """The full test with the most iterations left runs alone in the lead lane; the other
+    long tests share the chain lane, the short requests the bulk lane."""
+    reqs = [Request(0, 0.0, 4423, 4421, True), Request(1, 0.0, 9941, 9939, True),
+            Request(2, 0.0, 9689, 9687, True), Request(3, 0.0, 12379, 300, False)]
+    eng = ExactEngine()
+    srv = serve.Server(eng, step_ms=1e9, checkpoint_every=0)
+    done = {c.rid: c for c in srv.run(reqs, realtime=False)}
+    assert done[1].lane == "lead" and done[3].lane == "bulk"
+    assert {done[0].lane, done[2].lane} <= {"chain", "lead"}
+    for c in done.values():
+        assert c.status == serve.GL_OK and c.res64 == _exact(c.p, c.iterations)
+    assert done[0].is_prime and done[1].is_prime and done[2].is_prime
