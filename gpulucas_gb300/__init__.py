@@ -33,6 +33,7 @@ GL_ERR_IO = -9
 GL_ERR_CHECKPOINT = -10
 GL_ERR_STATE = -11
 GL_ERR_TOO_LARGE = -12
+GL_ERR_TIMEOUT = -13
 NOALLOC_MAX_N = 65536
 
 MODE_FUSED = 0

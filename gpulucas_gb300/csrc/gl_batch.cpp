@@ -109,7 +109,8 @@ int read_status(gl_batch* b, double* worst_err) {
     const double e = std::ldexp((double)b->h_status[i].maxerr64, -64);
     b->maxerr[i] = std::max(b->maxerr[i], e);
     worst = std::max(worst, e);
-    if (b->h_status[i].flags) st = GL_ERR_OVERFLOW;
+    if (b->h_status[i].flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
+    else if (b->h_status[i].flags && st != GL_ERR_TIMEOUT) st = GL_ERR_OVERFLOW;
     else if (e >= b->error_limit && st == GL_OK) st = GL_ERR_ROUNDOFF;
   }
   if (worst_err) *worst_err = worst;
@@ -192,6 +193,14 @@ int smallest_length(int p, Bits bits, int* N_out) {
   if (!best) return GL_ERR_SIZE;
   *N_out = best;
   return GL_OK;
+}
+
+// status of one test from the last status read
+int test_status_of(const gl_batch* b, int index) {
+  const unsigned fl = b->h_status[(size_t)index].flags;
+  if (fl & kStatusTimeout) return GL_ERR_TIMEOUT;
+  if (fl) return GL_ERR_OVERFLOW;
+  return b->maxerr[(size_t)index] >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK;
 }
 
 }  // namespace
@@ -381,10 +390,7 @@ int gl_batch_result(gl_batch* b, int index, gl_result* r, int* status) {
   r->is_prime = (pl->iters_done == (int64_t)pl->p - 2 && z) ? 1 : 0;
   r->res64 = res;
   r->max_roundoff = b->maxerr[(size_t)index];
-  if (status) {
-    const Status& s = b->h_status[(size_t)index];
-    *status = s.flags ? GL_ERR_OVERFLOW : (b->maxerr[(size_t)index] >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK);
-  }
+  if (status) *status = test_status_of(b, index);
   return GL_OK;
 }
 
@@ -392,8 +398,7 @@ int gl_batch_test_status(const gl_batch* b, int index, double* max_roundoff, int
   if (!b || index < 0 || index >= (int)b->plans.size()) return GL_ERR_ARG;
   const double e = b->maxerr[(size_t)index];
   if (max_roundoff) *max_roundoff = e;
-  if (status)
-    *status = b->h_status[(size_t)index].flags ? GL_ERR_OVERFLOW : (e >= b->error_limit ? GL_ERR_ROUNDOFF : GL_OK);
+  if (status) *status = test_status_of(b, index);
   return GL_OK;
 }
 

@@ -84,6 +84,15 @@ double line_ops(const LinePlan& lp) {
 
 int padded_stride(int L) { return L + (L >> 4) + 1; }
 
+int stage_offsets(const LinePlan& lp, int* off);
+
+// Shared memory of a row-pass CTA: four line buffers (the pair, ping-pong) and the copy of
+// the length-W stage twiddles.
+size_t row_smem(int W, const LinePlan& pw) {
+  int off[8];
+  return (size_t)4 * padded_stride(W) * 16 + (size_t)stage_offsets(pw, off) * sizeof(DevCplx);
+}
+
 // Radix caps of a layout chosen without timing: below 2^17 complex points a single test
 // cannot fill the device with one thread per radix-8 butterfly, and the timed search
 // picks radix-4 caps there (more warps per line); a batch member keeps radix 8 (the batch
@@ -109,7 +118,7 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
     if (W < 2) continue;
     LinePlan a, b;
     if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
-    const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = (size_t)4 * padded_stride(W) * 16;
+    const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = row_smem(W, a);
     if (smc > (size_t)kMaxDynSmem || smr > (size_t)kMaxDynSmem) continue;
     if ((H + kElemsPerThread - 1) / kElemsPerThread > 4 * kMaxThreads) continue;
     const double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
@@ -144,7 +153,7 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   g->ls_col = padded_stride(g->H);
   g->ls_row = padded_stride(g->W);
   g->sm_col = (size_t)2 * g->ls_col * 16;
-  g->sm_row = (size_t)4 * g->ls_row * 16;
+  g->sm_row = row_smem(g->W, g->pw);
   auto threads = [](int points, int per_thread, int cap) {
     int t = round_up32((points + per_thread - 1) / per_thread);
     return t < 64 ? 64 : (t > cap ? cap : t);
@@ -201,7 +210,7 @@ double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cuda
     a.ll = (long long*)buf[0]; a.flags = (const unsigned char*)buf[1]; a.span = (const unsigned char*)buf[2];
     a.A = (const double*)buf[3]; a.Ainv = (const double*)buf[4]; a.Z = (DevCplx*)buf[5];
     a.twK1 = (const DevCplx*)buf[6]; a.twPair = (const DevCplx*)buf[7]; a.twK2 = (const DevCplx*)buf[8];
-    a.twW = (const DevCplx*)buf[9]; a.twH = (const DevCplx*)buf[10];
+    a.twW = (const DevCplx*)buf[9]; a.twH = (const DevCplx*)buf[10]; a.twW_n = szw;
     a.digit = (int*)buf[11]; a.hi = (signed char*)buf[12]; a.status = (Status*)buf[13];
     for (int i = 0; i < 2 && ok; ++i) ok = launch_fused_iteration(a, g, s, false) == cudaSuccess;
     ok = ok && cudaEventRecord(e0, s) == cudaSuccess;
@@ -340,13 +349,12 @@ int read_status(gl_plan* pl, double* maxerr_out) {
   const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
   if (e > pl->run_maxerr) pl->run_maxerr = e;
   if (maxerr_out) *maxerr_out = e;
+  if (pl->h_status->flags & kStatusTimeout) return GL_ERR_TIMEOUT;
   if (pl->h_status->flags) return GL_ERR_OVERFLOW;
   if (e >= pl->error_limit) return GL_ERR_ROUNDOFF;
   return GL_OK;
 }
 
-// Host side of addPseudoBalanced + rebalanceIrrIntSEQGPU (IrrBaseBalanced.cu:117-169):
-// one balanced carry pass with the final carry wrapped into word 0.
 }  // namespace
 
 extern "C" {
@@ -368,6 +376,7 @@ const char* gl_error_string(int s) {
     case GL_ERR_CHECKPOINT: return "checkpoint does not match the test";
     case GL_ERR_STATE: return "call not valid in this state";
     case GL_ERR_TOO_LARGE: return "N exceeds 65536, the limit of gl_iterate_noalloc";
+    case GL_ERR_TIMEOUT: return "a bounded device-side wait ran out";
     default: return "unknown status";
   }
 }
@@ -570,6 +579,9 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     GL_TRYC(cudaMemcpyAsync(dK2, tK2.data(), sizeof(DevCplx) * M, cudaMemcpyHostToDevice, pl->stream));
     GL_TRYC(cudaStreamSynchronize(pl->stream));  // host tables go out of scope
     a.W = W; a.H = H; a.G = 1; a.pw = pl->fg.pw; a.ph = pl->fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
+    a.twW_n = (int)twW.size();
+    // the row pass copies the whole table behind its four line buffers
+    if ((size_t)4 * fg.ls_row * 16 + twW.size() * sizeof(DevCplx) != fg.sm_row) GL_TRY(GL_ERR_SIZE);
     GL_TRYC(set_fused_smem_limits(fg));
   }
   a.ll = ll; a.flags = fl; a.span = span; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;

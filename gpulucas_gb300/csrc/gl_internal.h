@@ -39,6 +39,7 @@ struct Status {
 };
 constexpr unsigned kStatusBig = 1u;    // |product| >= 2^51: doubles cannot hold it exactly
 constexpr unsigned kStatusSlice = 2u;  // product bits beyond what n+1 slices place
+constexpr unsigned kStatusTimeout = 4u; // a bounded device-side wait ran out (kernel returned)
 
 // Geometry of the fused form: the N/2 complex points are an H x W array
 // (element m = m1 + W*m2); each column pass CTA takes one column (G = 1), each row
@@ -74,6 +75,7 @@ struct IterArgs {
   DevCplx* Z2;                // M complex (plain: ping-pong)
   const DevCplx* twM;         // exp(-2 pi i t/M), t < M
   const DevCplx* twW;         // stage-ordered twiddles of the length-W line DFT
+  int twW_n;                  // entries of twW (the row pass copies them to shared memory)
   const DevCplx* twH;         // stage-ordered twiddles of the length-H line DFT
   const DevCplx* twK1;        // w_M^(m1 k2) at m1*H + k2 (column pass output)
   const DevCplx* twPair;      // w_M^(k2 + H k1) at k2*W + k1 (real-signal split)

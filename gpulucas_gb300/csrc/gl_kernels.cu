@@ -36,6 +36,47 @@ __device__ __forceinline__ cplx ldc(const DevCplx* p) {
 __device__ __forceinline__ void st(DevCplx* p, cplx v) {
   *reinterpret_cast<double2*>(p) = make_double2(v.re, v.im);
 }
+// a twiddle from the global table (read-only path) or from a shared-memory copy
+__device__ __forceinline__ cplx tw_at(const DevCplx* p) { return ld(p); }
+__device__ __forceinline__ cplx tw_at(const cplx* p) { return *p; }
+
+// ---------------------------------------------------------------------------
+// Bulk copies global -> shared (cp.async.bulk, the TMA's untiled form) completing on an
+// mbarrier.  Every wait is bounded: after kWaitTries polls (each may suspend the thread
+// for a while) it reports failure and the caller returns with kStatusTimeout.
+// ---------------------------------------------------------------------------
+constexpr int kWaitTries = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// one thread: expect `bytes` on the barrier and start the copy (16-byte aligned
+// addresses, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < kWaitTries; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 
 // ---------------------------------------------------------------------------
 // Shared-memory line FFTs.  Element i of a line sits at pad(i) = i + i/16: the
@@ -50,9 +91,9 @@ __device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
 // p Ns].  Power-of-two radices run the layered FMA-merged DIT (its per-level twiddle
 // values come from the stage-ordered table at off + v Ns + k); odd radices multiply
 // by w^q from the table and run DFT_R.
-template <int R, int S>
+template <int R, int S, typename TW>
 __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cplx* __restrict__ dst, int nlines,
-                                               int ls, int L, int Ns, const DevCplx* __restrict__ tw) {
+                                               int ls, int L, int Ns, const TW* __restrict__ tw) {
   constexpr bool POW2 = (R & (R - 1)) == 0;
   constexpr int NV = POW2 ? (R == 2 ? 1 : R / 2) : R - 1;
   const int LR = L / R;
@@ -69,7 +110,7 @@ __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cpl
       cplx tv[NV];
 #pragma unroll
       for (int i = 0; i < NV; ++i) {
-        const cplx t = ld(tw + (size_t)i * Ns + k);
+        const cplx t = tw_at(tw + (size_t)i * Ns + k);
         tv[i] = S < 0 ? t : conj(t);
       }
       if constexpr (POW2) {
@@ -93,12 +134,12 @@ __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cpl
 
 // Transforms nlines lines held in `a` (line stride ls) using `b` as the second buffer;
 // returns the buffer that holds the result.
-template <int S>
+template <int S, typename TW>
 __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, const LinePlan& lp,
-                                          const DevCplx* tw) {
+                                          const TW* tw) {
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
-    const DevCplx* st = tw + lp.off[s];
+    const TW* st = tw + lp.off[s];
     static_assert(kMaxRadix == 8, "line plans use radices 2, 4, 8, 3, 5, 7");
     switch (lp.radix[s]) {
       case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, st); break;
@@ -214,21 +255,37 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
   col_fwd_body<FROM_STATE, NC>(a, blockIdx.x);
 }
 
+// The row pass's stage twiddles (a few KB) are copied into shared memory behind the four
+// line buffers by one bulk copy, issued before the rows are loaded so the two overlap;
+// both DFTs of the pair, forward and inverse, then read twiddles from shared memory.
 __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 .. H/2 */) {
   extern __shared__ cplx smem[];
+  __shared__ alignas(8) uint64_t tw_bar;
   const int W = a.W, H = a.H;
   const int ls = a.ls_row;
   const int ra = c, rb = H - c;
   const bool self = (c == 0) || (2 * c == H);
   const int nl = self ? 1 : 2;
   cplx* buf1 = smem + 2 * ls;
+  cplx* tws = smem + 4 * ls;
+  if (threadIdx.x == 0) mbar_init(&tw_bar);
+  __syncthreads();
+  if (threadIdx.x == 0) bulk_load(tws, a.twW, (uint32_t)a.twW_n * (uint32_t)sizeof(DevCplx), &tw_bar);
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
     const int l = idx >= W;
     const int k1 = idx - l * W;
     smem[l * ls + pad(k1)] = ldc(a.Z + (size_t)(l ? rb : ra) * W + k1);
   }
-  __syncthreads();
-  cplx* sp = line_fft<-1>(smem, buf1, nl, ls, a.pw, a.twW);
+  const bool ok = mbar_wait(&tw_bar, 0);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) {
+      atomicOr(&a.status->flags, kStatusTimeout);
+      mbar_wait(&tw_bar, 0);  // the copy may still land in this CTA's shared memory
+    }
+    return;
+  }
+  const cplx* twc = tws;
+  cplx* sp = line_fft<-1>(smem, buf1, nl, ls, a.pw, twc);
   cplx* other = sp == smem ? buf1 : smem;
   const DevCplx* twp = a.twPair + (size_t)ra * W;
   if (!self) {
@@ -259,7 +316,7 @@ __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 
     }
   }
   __syncthreads();
-  const cplx* res = line_fft<+1>(sp, other, nl, ls, a.pw, a.twW);
+  const cplx* res = line_fft<+1>(sp, other, nl, ls, a.pw, twc);
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
     const int l = idx >= W;
     const int m1 = idx - l * W;

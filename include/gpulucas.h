@@ -36,6 +36,8 @@ extern "C" {
 #define GL_ERR_CHECKPOINT -10 /* checkpoint does not match this test */
 #define GL_ERR_STATE -11     /* call not valid in the plan's current state */
 #define GL_ERR_TOO_LARGE -12 /* N above the limit of the no-allocation entry point */
+#define GL_ERR_TIMEOUT -13   /* a bounded wait in a kernel ran out (an asynchronous copy never
+                                completed); the kernel returned without computing */
 
 /* execution forms */
 #define GL_MODE_FUSED 0      /* 3 fused kernels per iteration (the product form) */
