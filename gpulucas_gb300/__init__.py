@@ -45,7 +45,7 @@ class PlanOpts(ctypes.Structure):
                 ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
                 ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("batch_layout", ctypes.c_int),
                 ("high_priority", ctypes.c_int), ("max_radix_col", ctypes.c_int),
-                ("max_radix_row", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("max_radix_row", ctypes.c_int), ("resident", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -53,7 +53,8 @@ class PlanInfo(ctypes.Structure):
                 ("carry_depth", ctypes.c_int), ("mode", ctypes.c_int), ("fft_w", ctypes.c_int),
                 ("fft_h", ctypes.c_int), ("cols_per_cta", ctypes.c_int), ("radix_w", ctypes.c_int * 8),
                 ("radix_h", ctypes.c_int * 8), ("threads_col", ctypes.c_int), ("threads_row", ctypes.c_int),
-                ("smem_col", ctypes.c_int), ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t)]
+                ("smem_col", ctypes.c_int), ("smem_row", ctypes.c_int), ("device_bytes", ctypes.c_size_t),
+                ("resident_ctas", ctypes.c_int), ("resident_smem", ctypes.c_int)]
 
 
 class BatchInfo(ctypes.Structure):

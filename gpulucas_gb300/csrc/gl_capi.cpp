@@ -316,6 +316,14 @@ int enqueue(gl_plan* pl, int64_t k) {
     if ((rc = launch_iterations(pl, 1)) != GL_OK) return rc;
     --k;
   }
+  if (pl->resident) {  // one cluster launch runs them all
+    while (k > 0) {
+      const int chunk = (int)std::min<int64_t>(k, 1 << 30);
+      GL_CUDA(launch_resident(pl->args, pl->rg, chunk, pl->stream));
+      k -= chunk;
+    }
+    return GL_OK;
+  }
   if (pl->use_graphs && k >= kGraphBatch) {
     if (!pl->gexec) {
       cudaGraph_t graph = nullptr;
@@ -455,6 +463,31 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   if (sms_override > 0) sms = sms_override;
   int force_h = o.fft_h, cap_c = kMaxRadix, cap_r = kMaxRadix;
   model_caps(M, o, sms_override, &cap_c, &cap_r);
+  // Short lengths: the resident form (one cluster, the whole test in shared memory) when
+  // a layout with W divisible by the cluster size fits; it replaces the layout search.
+  bool resident = false;
+  ResidentGeom rg{};
+  if (o.mode == GL_MODE_FUSED && !sms_override && !force_h &&
+      (o.resident > 0 ? N <= kResidentMaxN : (o.resident == 0 && N <= kResidentAutoN))) {
+    // radix 4: each CTA's lines are short, and more, shorter butterflies keep more warps
+    // issuing FP64 work (measured: 13.8 us at N = 2048 against 16.6 us with radix 8)
+    const int rcap = o.max_radix_col ? o.max_radix_col : 4, wcap = o.max_radix_row ? o.max_radix_row : 4;
+    for (const auto& c : ranked_layouts(M, sms)) {
+      FusedGeom t{};
+      if (choose_fused_geom(M, c.second, sms, &t, rcap, wcap) != GL_OK) continue;
+      int offh[8], offw[8];
+      const int nh = stage_offsets(t.ph, offh), nw = stage_offsets(t.pw, offw);
+      if (resident_geom(t, nh, nw, n, &rg) == cudaSuccess) {
+        resident = true;
+        force_h = c.second;
+        cap_c = rcap;
+        cap_r = wcap;
+        break;
+      }
+    }
+    cudaGetLastError();
+  }
+  if (o.resident > 0 && !resident) return GL_ERR_SIZE;
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
@@ -583,6 +616,11 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     // the row pass copies the whole table behind its four line buffers
     if ((size_t)4 * fg.ls_row * 16 + twW.size() * sizeof(DevCplx) != fg.sm_row) GL_TRY(GL_ERR_SIZE);
     GL_TRYC(set_fused_smem_limits(fg));
+    if (resident) {
+      if (rg.twH_n != (int)twH.size() || rg.twW_n != (int)twW.size()) GL_TRY(GL_ERR_SIZE);
+      pl->resident = true;
+      pl->rg = rg;
+    }
   }
   a.ll = ll; a.flags = fl; a.span = span; a.A = dA; a.Ainv = dAi; a.Z = Z; a.Z2 = Z2;
   a.twM = dtwM; a.twW = dtwW; a.twH = dtwH; a.twK1 = dK1; a.twPair = dPair; a.twK2 = dK2;
@@ -658,6 +696,8 @@ int gl_plan_get_info(const gl_plan* pl, gl_plan_info* info) {
     for (int i = 0; i < pl->pg.nst && i < 8; ++i) info->radix_w[i] = pl->pg.radix[i];
   }
   info->device_bytes = pl->device_bytes;
+  info->resident_ctas = pl->resident ? pl->rg.C : 0;
+  info->resident_smem = pl->resident ? pl->rg.smem : 0;
   return GL_OK;
 }
 

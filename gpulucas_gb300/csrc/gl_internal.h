@@ -86,6 +86,30 @@ struct IterArgs {
   LinePlan pw, ph;
 };
 
+// Resident form of a fused plan (short lengths): one thread-block cluster of C CTAs keeps
+// the products, the work arrays and every table of the test in distributed shared memory
+// and runs many iterations per launch, the three passes separated by cluster barriers.
+// CTA r owns columns [r cw, (r+1) cw) and the row pairs c = r, r + C, ... <= H/2.
+// Shared-memory regions, byte offsets (all 16-byte aligned):
+//   zc, zc2  column lines (cw x ls_col complex, ping-pong)   zr, zr2  row lines (2 npl x ls_row)
+//   ll, A, Ai  own columns' products / weights (cw x 2H, 8 B)  fl, sp  flags / span bytes
+//   K1  own columns' w^(m1 k2) (cw x H)   pr  own pairs' split coefficients (npl x W)
+//   K2  own rows' w^(m1 k2) (2 npl x W)   twH, twW  stage twiddle tables
+struct ResidentGeom {
+  int C, cw, npl, threads;
+  int smem;
+  int o_zc, o_zc2, o_zr, o_zr2, o_ll, o_A, o_Ai, o_fl, o_sp, o_K1, o_pr, o_K2, o_twH, o_twW;
+  int twH_n, twW_n;
+};
+constexpr int kResidentThreads = 256;
+constexpr int kResidentMaxN = 32768;   // largest N the resident form is tried at (opts.resident = 1)
+constexpr int kResidentAutoN = 4096;   // used by default up to here: measured faster than the
+                                       // three-launch form (13.8 vs 18.3 us at N = 2048, 16.1 vs
+                                       // 19.6 us at 4096; slower from 8192 on)
+// smallest cluster first; fills r and returns cudaSuccess if the layout fits one cluster
+cudaError_t resident_geom(const FusedGeom& g, int twH_n, int twW_n, int n, ResidentGeom* r);
+cudaError_t launch_resident(const IterArgs& a, const ResidentGeom& r, int iters, cudaStream_t s);
+
 // A batch of fused-form tests advanced by one set of launches: the descriptor table of
 // every test's arguments (device) and the unit maps (test, local column / row pair).
 struct BatchLaunch {

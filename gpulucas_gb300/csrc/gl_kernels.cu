@@ -18,6 +18,8 @@
 //
 // Plain form: one kernel per reference step, the FFT as one global-memory Stockham
 // stage per launch (radix <= 4), state = (digit, hi) as in the reference.
+#include <cooperative_groups.h>
+
 #include "gl_device.cuh"
 #include "gl_internal.h"
 
@@ -693,6 +695,322 @@ __global__ void k_probe_dfma(double* out, long long iters, double a, double b) {
 cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s) {
   k_probe_dfma<<<blocks, threads, 0, s>>>(out, iters, 0.999999999, 1e-12);
   return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// Resident form: one cluster holds the test (see ResidentGeom in gl_internal.h).  Per
+// iteration: (A) each CTA dices its columns' products (the halo words of the columns
+// below come from the owners' shared memory), weights, runs the column DFTs and scatters
+// the twiddled columns into the row owners' row lines; cluster barrier; (B) each CTA
+// runs its row pairs (DFTs, split + square, inverse DFTs) and scatters the twiddled rows
+// into the column owners' column lines; cluster barrier; (C) inverse column DFTs, unweight,
+// round, -2, products into shared memory; cluster barrier.  The arithmetic is the fused
+// kernels' (same line plans, tables and rounding), so the products are identical.
+// ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
+struct ResidentArgs {
+  IterArgs a;
+  ResidentGeom g;
+  int iters;
+};
+
+template <int NC>
+__global__ void __launch_bounds__(kResidentThreads, 1) k_resident(const __grid_constant__ ResidentArgs ra) {
+  cg::cluster_group cl = cg::this_cluster();
+  const IterArgs& a = ra.a;
+  const ResidentGeom& g = ra.g;
+  extern __shared__ __align__(16) unsigned char rsm[];
+  const int rank = (int)cl.block_rank();
+  const int C = g.C, cw = g.cw, H = a.H, W = a.W, N = a.N;
+  const int lsc = a.ls_col, lsr = a.ls_row;
+  const int c0 = rank * cw;
+  const int npl = (H / 2 - rank) / C + 1;  // my pairs c = rank + C lp <= H/2 (rank < C <= H/2 + 1)
+  cplx* zc = reinterpret_cast<cplx*>(rsm + g.o_zc);
+  cplx* zc2 = reinterpret_cast<cplx*>(rsm + g.o_zc2);
+  cplx* zr = reinterpret_cast<cplx*>(rsm + g.o_zr);
+  cplx* zr2 = reinterpret_cast<cplx*>(rsm + g.o_zr2);
+  long long* ll = reinterpret_cast<long long*>(rsm + g.o_ll);
+  double* A = reinterpret_cast<double*>(rsm + g.o_A);
+  double* Ai = reinterpret_cast<double*>(rsm + g.o_Ai);
+  unsigned char* fl = rsm + g.o_fl;
+  unsigned char* sp = rsm + g.o_sp;
+  cplx* K1 = reinterpret_cast<cplx*>(rsm + g.o_K1);
+  cplx* pr = reinterpret_cast<cplx*>(rsm + g.o_pr);
+  cplx* K2 = reinterpret_cast<cplx*>(rsm + g.o_K2);
+  cplx* twH = reinterpret_cast<cplx*>(rsm + g.o_twH);
+  cplx* twW = reinterpret_cast<cplx*>(rsm + g.o_twW);
+  const int T = blockDim.x, tid = threadIdx.x;
+
+  // own slices of the state and the tables (column-major per-word arrays: my columns
+  // are one contiguous block), whole stage tables
+  const int nw = cw * 2 * H;            // my words
+  const size_t wbase = (size_t)c0 * 2 * H;
+  for (int i = tid; i < nw; i += T) {
+    ll[i] = a.ll[wbase + i];
+    A[i] = a.A[wbase + i];
+    Ai[i] = a.Ainv[wbase + i];
+    fl[i] = a.flags[wbase + i];
+    sp[i] = a.span[wbase + i];
+  }
+  for (int i = tid; i < cw * H; i += T) K1[i] = ld(a.twK1 + (size_t)c0 * H + i);
+  for (int i = tid; i < npl * W; i += T) {
+    const int lp = i / W, t = i - lp * W;
+    pr[i] = ld(a.twPair + (size_t)(rank + C * lp) * W + t);
+  }
+  for (int i = tid; i < 2 * npl * W; i += T) {
+    const int s = i / W, m1 = i - s * W;
+    const int c = rank + C * (s >> 1);
+    const int row = (s & 1) ? (H - c) % H : c;
+    K2[i] = ld(a.twK2 + (size_t)row * W + m1);
+  }
+  for (int i = tid; i < g.twH_n; i += T) twH[i] = ld(a.twH + i);
+  for (int i = tid; i < g.twW_n; i += T) twW[i] = ld(a.twW + i);
+  cl.sync();
+
+  // word j's owner and local index
+  auto where = [&](int j, int* owner) {
+    const int m = j >> 1;
+    const int m2 = m / W;
+    const int m1 = m - m2 * W;
+    const int o = m1 / cw;
+    *owner = o;
+    return 2 * ((m1 - o * cw) * H + m2) + (j & 1);
+  };
+
+  for (int it = 0; it < ra.iters; ++it) {
+    // (A) dice, weight, column DFTs, twiddle, scatter to the row owners
+    for (int idx = tid; idx < cw * H; idx += T) {
+      const int lc = idx / H, m2 = idx - lc * H;
+      const int m1 = c0 + lc;
+      const int j0 = 2 * (m1 + W * m2);
+      const int s0 = 2 * idx;  // == 2 (lc H + m2)
+      long long P[NC + 3];
+      P[0] = ll[s0 + 1];
+      P[1] = ll[s0];
+#pragma unroll
+      for (int k = 2; k < NC + 3; ++k) {
+        int j = j0 + 1 - k;
+        if (j < 0) j += N;
+        int o;
+        const int li = where(j, &o);
+        P[k] = *cl.map_shared_rank(ll + li, o);
+      }
+      const int jm = j0 == 0 ? N - 1 : j0 - 1;
+      int om;
+      const int lm = where(jm, &om);
+      const uint32_t f0 = fl[s0], f1 = fl[s0 + 1], fm = *cl.map_shared_rank(fl + lm, om);
+      const int LO = a.LO;
+      auto dice_at = [&](uint32_t f, int off) {
+        const long long mask = (1ll << (LO + (int)(f & 1))) - 1;
+        const long long v = P[off];
+        long long sum = v < 0 ? -((-v) & mask) : (v & mask);
+        int shift = 0;
+#pragma unroll
+        for (int i = 1; i <= NC; ++i) {
+          shift += LO + (int)((f >> i) & 1);
+          const long long w = P[off + i];
+          sum += shift >= 63 ? 0 : (w < 0 ? -(((-w) >> shift) & mask) : ((w >> shift) & mask));
+        }
+        return sum;
+      };
+      const long long sw1 = dice_at(f1, 0), sw0 = dice_at(f0, 1), sm1 = dice_at(fm, 2);
+      int dm, hm, d0, h0, d1, h1;
+      balanced_split(sm1, LO + (int)(fm & 1), &dm, &hm);
+      balanced_split(sw0, LO + (int)(f0 & 1), &d0, &h0);
+      balanced_split(sw1, LO + (int)(f1 & 1), &d1, &h1);
+      zc[lc * lsc + pad(m2)] = mk(A[s0] * dbl_from_int(d0 + hm), A[s0 + 1] * dbl_from_int(d1 + h0));
+    }
+    __syncthreads();
+    {
+      const cplx* res = line_fft<-1>(zc, zc2, cw, lsc, a.ph, (const cplx*)twH);
+      for (int idx = tid; idx < cw * H; idx += T) {
+        const int lc = idx / H, k2 = idx - lc * H;
+        const cplx v = cmul(res[lc * lsc + pad(k2)], K1[idx]);
+        const int c = k2 <= H / 2 ? k2 : H - k2;
+        const int slot = 2 * (c / C) + (k2 == c ? 0 : 1);
+        *cl.map_shared_rank(zr + slot * lsr + pad(c0 + lc), c % C) = v;
+      }
+    }
+    cl.sync();
+
+    // (B) row pairs
+    {
+      const int nl = 2 * npl;
+      cplx* s1 = line_fft<-1>(zr, zr2, nl, lsr, a.pw, (const cplx*)twW);
+      cplx* other = s1 == zr ? zr2 : zr;
+      for (int idx = tid; idx < npl * W; idx += T) {
+        const int lp = idx / W, t = idx - lp * W;
+        const int c = rank + C * lp;
+        cplx* L0 = s1 + (2 * lp) * lsr;
+        cplx* L1 = L0 + lsr;
+        const cplx cf = pr[idx];
+        cplx vk, vkp;
+        if (c != 0 && 2 * c != H) {
+          const int tp = W - 1 - t;
+          pair_square(L0[pad(t)], L1[pad(tp)], cf, &vk, &vkp);
+          L0[pad(t)] = vk;
+          L1[pad(tp)] = vkp;
+        } else if (c == 0) {
+          if (t <= W / 2) {
+            const int tp = (W - t) % W;
+            pair_square(L0[pad(t)], L0[pad(tp)], cf, &vk, &vkp);
+            L0[pad(t)] = vk;
+            if (tp != t) L0[pad(tp)] = vkp;
+          }
+        } else if (t < (W + 1) / 2) {
+          const int tp = W - 1 - t;
+          pair_square(L0[pad(t)], L0[pad(tp)], cf, &vk, &vkp);
+          L0[pad(t)] = vk;
+          if (tp != t) L0[pad(tp)] = vkp;
+        }
+      }
+      __syncthreads();
+      const cplx* res = line_fft<+1>(s1, other, nl, lsr, a.pw, (const cplx*)twW);
+      for (int idx = tid; idx < nl * W; idx += T) {
+        const int s = idx / W, m1 = idx - s * W;
+        const int c = rank + C * (s >> 1);
+        if ((s & 1) && (c == 0 || 2 * c == H)) continue;  // a self-paired row has one line
+        const int row = (s & 1) ? H - c : c;
+        const cplx v = cmulc(res[s * lsr + pad(m1)], K2[idx]);
+        const int o = m1 / cw;
+        *cl.map_shared_rank(zc + (m1 - o * cw) * lsc + pad(row), o) = v;
+      }
+    }
+    cl.sync();
+
+    // (C) inverse column DFTs, unweight, round, -2
+    {
+      const cplx* res = line_fft<+1>(zc, zc2, cw, lsc, a.ph, (const cplx*)twH);
+      unsigned long long emax = 0;
+      unsigned flg = 0;
+      for (int idx = tid; idx < cw * H; idx += T) {
+        const int lc = idx / H, m2 = idx - lc * H;
+        const int s0 = 2 * idx;
+        const cplx v = res[lc * lsc + pad(m2)];
+        long long r0 = round_word(v.re * Ai[s0], sp[s0], &emax, &flg);
+        const long long r1 = round_word(v.im * Ai[s0 + 1], sp[s0 + 1], &emax, &flg);
+        if (rank == 0 && idx == 0) r0 -= 2;  // word 0
+        ll[s0] = r0;
+        ll[s0 + 1] = r1;
+      }
+      finish_status(a, emax, flg);
+    }
+    cl.sync();
+  }
+  for (int i = tid; i < nw; i += T) a.ll[wbase + i] = ll[i];
+}
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+template <int NC>
+static cudaError_t resident_attrs(int smem, int C, cudaLaunchConfig_t* cfg, int* clusters) {
+  cudaError_t e = cudaFuncSetAttribute(k_resident<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  if (C > 8 && (e = cudaFuncSetAttribute(k_resident<NC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) !=
+                   cudaSuccess)
+    return e;
+  return cudaOccupancyMaxActiveClusters(clusters, k_resident<NC>, cfg);
+}
+
+static cudaError_t resident_fits(int n, int smem, int C, int* clusters) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kResidentThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  switch (n) {
+    case 2: return resident_attrs<2>(smem, C, &cfg, clusters);
+    case 3: return resident_attrs<3>(smem, C, &cfg, clusters);
+    case 4: return resident_attrs<4>(smem, C, &cfg, clusters);
+    case 5: return resident_attrs<5>(smem, C, &cfg, clusters);
+    default: return resident_attrs<6>(smem, C, &cfg, clusters);
+  }
+}
+
+cudaError_t resident_geom(const FusedGeom& fg, int twH_n, int twW_n, int n, ResidentGeom* r) {
+  const int H = fg.H, W = fg.W;
+  for (int C : {8, 16}) {
+    if (W % C || H / 2 + 1 < C) continue;
+    ResidentGeom g{};
+    g.C = C;
+    g.cw = W / C;
+    g.npl = (H / 2) / C + 1;
+    g.threads = kResidentThreads;
+    g.twH_n = twH_n;
+    g.twW_n = twW_n;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t at = o;
+      o = align16(o + bytes);
+      return (int)at;
+    };
+    const size_t colb = (size_t)g.cw * fg.ls_col * 16, rowb = (size_t)2 * g.npl * fg.ls_row * 16;
+    const size_t words = (size_t)g.cw * 2 * H;
+    g.o_zc = take(colb);
+    g.o_zc2 = take(colb);
+    g.o_zr = take(rowb);
+    g.o_zr2 = take(rowb);
+    g.o_ll = take(words * 8);
+    g.o_A = take(words * 8);
+    g.o_Ai = take(words * 8);
+    g.o_fl = take(words);
+    g.o_sp = take(words);
+    g.o_K1 = take((size_t)g.cw * H * 16);
+    g.o_pr = take((size_t)g.npl * W * 16);
+    g.o_K2 = take((size_t)2 * g.npl * W * 16);
+    g.o_twH = take((size_t)twH_n * 16);
+    g.o_twW = take((size_t)twW_n * 16);
+    if (o > (size_t)200 * 1024) continue;
+    g.smem = (int)o;
+    int clusters = 0;
+    if (resident_fits(n, g.smem, C, &clusters) != cudaSuccess) {
+      cudaGetLastError();  // clear a refused configuration
+      continue;
+    }
+    if (clusters < 1) continue;
+    *r = g;
+    return cudaSuccess;
+  }
+  return cudaErrorInvalidConfiguration;
+}
+
+template <int NC>
+static cudaError_t launch_resident_nc(const ResidentArgs& ra, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ra.g.C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(ra.g.C);
+  cfg.blockDim = dim3(ra.g.threads);
+  cfg.dynamicSmemBytes = ra.g.smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_resident<NC>, ra);
+}
+
+cudaError_t launch_resident(const IterArgs& a, const ResidentGeom& g, int iters, cudaStream_t s) {
+  ResidentArgs ra;
+  ra.a = a;
+  ra.g = g;
+  ra.iters = iters;
+  switch (a.n) {
+    case 2: return launch_resident_nc<2>(ra, s);
+    case 3: return launch_resident_nc<3>(ra, s);
+    case 4: return launch_resident_nc<4>(ra, s);
+    case 5: return launch_resident_nc<5>(ra, s);
+    default: return launch_resident_nc<6>(ra, s);
+  }
 }
 
 }  // namespace gl

@@ -8,6 +8,7 @@
 using gl::FusedGeom;
 using gl::IterArgs;
 using gl::PlainGeom;
+using gl::ResidentGeom;
 using gl::Status;
 
 struct gl_plan {
@@ -30,6 +31,8 @@ struct gl_plan {
   int gexec_iters = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t device_bytes = 0;
+  bool resident = false;        // short length: whole check intervals in one cluster
+  ResidentGeom rg{};
   uint8_t* rscratch = nullptr;  // device scratch of the residue kernels
   int32_t* h_res = nullptr;     // pinned: 64 canonical head digits, scalars, flags
 };

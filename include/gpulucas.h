@@ -60,7 +60,11 @@ typedef struct {
                               scheduled ahead of other work */
     int max_radix_col;     /* fused form: largest radix of the column / row line plans */
     int max_radix_row;     /* (8, 4 or 2; 0 = 8, or the autotuner's choice) */
-    int reserved[3];
+    int resident;          /* fused form, short lengths: run whole check intervals in one
+                              thread-block cluster holding the test in shared memory;
+                              0 = by default up to N = 4096 (where it is faster),
+                              1 = require (N <= 32768), -1 = never */
+    int reserved[2];
 } gl_plan_opts;
 
 typedef struct {
@@ -74,6 +78,8 @@ typedef struct {
     int threads_col, threads_row;  /* CTA sizes of the column and row passes */
     int smem_col, smem_row;        /* dynamic shared memory bytes of those passes */
     size_t device_bytes;   /* device memory held by the plan */
+    int resident_ctas;     /* CTAs of the resident form's cluster, 0 if not used */
+    int resident_smem;     /* its shared memory per CTA */
 } gl_plan_info;
 
 typedef struct {

@@ -91,12 +91,34 @@ def test_device_residue_matches_oracle(gl, orc, p, N, mode):
             assert pl.res64_zero() == (r, z)
 
 
+@pytest.mark.parametrize("p,N", [(44497, 2048), (12379, 640), (86243, 4096), (100003, 5184), (300007, 15360),
+                                 (600011, 32768)])
+def test_resident_form_matches_oracle(gl, orc, p, N):
+    """Short lengths run whole check intervals in one cluster (state and tables in
+    distributed shared memory); the products equal the oracle's and the three-launch
+    form's, across several launches and a state load."""
+    with gl.Plan(p, N, resident=1) as pl, gl.Plan(p, N, resident=-1) as ref:
+        assert pl.info.resident_ctas in (8, 16) and ref.info.resident_ctas == 0
+        o = orc.IBDWT(p, N)
+        for k in (1, 5, 37):
+            pl.iterate(k)
+            ref.iterate(k)
+            o.iterate(k)
+            assert (pl.products() == o.ll()).all() and (ref.products() == o.ll()).all()
+        d, h = pl.carry_state()
+        pl.set_carry_state(d, h, 43)   # the next iteration loads the state, then resident
+        pl.iterate(20)
+        o.iterate(20)
+        assert (pl.products() == o.ll()).all()
+        assert pl.res64() == orc.Exact(p).iterate(63).res64()
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432), (2976221, 163840)])
 @pytest.mark.parametrize("caps", [(4, 4), (2, 2), (4, 8), (8, 2)])
 def test_radix_capped_layouts_match_oracle(gl, orc, p, N, caps):
     """Line plans with smaller radices (more threads per line, for short lengths) give
     the same integer products as the oracle."""
-    with gl.Plan(p, N, max_radix_col=caps[0], max_radix_row=caps[1], autotune=0) as pl:
+    with gl.Plan(p, N, max_radix_col=caps[0], max_radix_row=caps[1], autotune=0, resident=-1) as pl:
         assert max(pl.info.radix_h) <= max(caps[0], 7) and max(pl.info.radix_w) <= max(caps[1], 7)
         o = orc.IBDWT(p, N)
         pl.iterate(9)
