@@ -193,7 +193,8 @@ double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cuda
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
                           16 * (size_t)M, 16 * (size_t)M, 16 * (size_t)M, 16 * (size_t)M,
-                          16 * (size_t)szw, 16 * (size_t)szh, sizeof(int) * N, (size_t)N, sizeof(Status)};
+                          16 * (size_t)szw, 16 * (size_t)szh, sizeof(int) * N, (size_t)N, sizeof(Status),
+                          16 * (size_t)M};
   constexpr int nb = sizeof(bytes) / sizeof(bytes[0]);
   void* buf[nb] = {};
   double ms = -1.0;
@@ -212,6 +213,7 @@ double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cuda
     a.twK1 = (const DevCplx*)buf[6]; a.twPair = (const DevCplx*)buf[7]; a.twK2 = (const DevCplx*)buf[8];
     a.twW = (const DevCplx*)buf[9]; a.twH = (const DevCplx*)buf[10]; a.twW_n = szw;
     a.digit = (int*)buf[11]; a.hi = (signed char*)buf[12]; a.status = (Status*)buf[13];
+    a.Z2 = (DevCplx*)buf[14];
     for (int i = 0; i < 2 && ok; ++i) ok = launch_fused_iteration(a, g, s, false) == cudaSuccess;
     ok = ok && cudaEventRecord(e0, s) == cudaSuccess;
     for (int i = 0; i < iters && ok; ++i) ok = launch_fused_iteration(a, g, s, false) == cudaSuccess;
@@ -595,6 +597,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
         }
     });
     pl->fg = fg;
+    GL_TRY(dev_alloc(pl, &Z2, M));  // the row pass's output, column-major
     GL_TRY(dev_alloc(pl, &span, N));
     GL_TRY(dev_alloc(pl, &dtwW, twW.size()));
     GL_TRY(dev_alloc(pl, &dtwH, twH.size()));
@@ -667,7 +670,7 @@ int gl_plan_describe(int p, int N, const gl_plan_opts* opts, gl_plan_info* info)
     const size_t M = tmp.M, N8 = (size_t)N * 8;
     const size_t stages = (size_t)stage_offsets(tmp.fg.pw, tmp.fg.pw.off) + stage_offsets(tmp.fg.ph, tmp.fg.ph.off);
     info->device_bytes = N8 /*ll*/ + 2 * (size_t)N /*flags, span*/ + 2 * N8 /*A, Ainv*/ +
-                         4 * M * 16 /*Z, 3 twiddle tables*/ + stages * 16 + (size_t)N * 5 /*digit, hi*/ +
+                         5 * M * 16 /*Z, Z2, 3 twiddle tables*/ + stages * 16 + (size_t)N * 5 /*digit, hi*/ +
                          sizeof(Status) + residue_scratch_bytes(N);
   }
   return r;

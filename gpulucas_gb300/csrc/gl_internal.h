@@ -72,7 +72,7 @@ struct IterArgs {
   const double* A;            // N weights (fused: column-major)
   const double* Ainv;         // N inverse weights with 1/(2N) folded in (fused: column-major)
   DevCplx* Z;                 // M complex work array [H][W]
-  DevCplx* Z2;                // M complex (plain: ping-pong)
+  DevCplx* Z2;                // M complex: plain, ping-pong; fused, the row pass's output [W][H]
   const DevCplx* twM;         // exp(-2 pi i t/M), t < M
   const DevCplx* twW;         // stage-ordered twiddles of the length-W line DFT
   int twW_n;                  // entries of twW (the row pass copies them to shared memory)

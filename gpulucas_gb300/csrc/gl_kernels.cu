@@ -10,7 +10,9 @@
 //   k_row_sq  : per row pair (k2, H-k2): length-W DFTs over m1, the real-signal split
 //               and pointwise square (ComplexPointwiseSqr, gpuLucas.cu:647-665, for the
 //               D2Z/Z2D pair of gpuLucas.cu:869-877), inverse length-W DFTs, twiddle
-//               w_M^-(m1 k2)
+//               w_M^-(m1 k2), stored column-major into a second work array so that the
+//               inverse column pass reads its column contiguously (the transposing
+//               accesses are stores, which do not stall the issuing warp)
 //   k_col_inv : per column: inverse length-H DFT, unweight, subtract 2 at word 0, round
 //               half-even to int64, round-off max (invDWTproductMinus2,
 //               gpuLucas.cu:774-805)
@@ -323,7 +325,7 @@ __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 
     const int l = idx >= W;
     const int m1 = idx - l * W;
     const int row = l ? rb : ra;
-    st(a.Z + (size_t)row * W + m1, cmulc(res[l * ls + pad(m1)], ld(a.twK2 + (size_t)row * W + m1)));
+    st(a.Z2 + (size_t)m1 * H + row, cmulc(res[l * ls + pad(m1)], ld(a.twK2 + (size_t)row * W + m1)));
   }
 }
 
@@ -368,10 +370,10 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
 
 __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   extern __shared__ cplx smem[];
-  const int H = a.H, W = a.W;
+  const int H = a.H;
   const int ls = a.ls_col;
   cplx* buf1 = smem + ls;
-  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z + (size_t)k2 * W + m1);
+  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z2 + (size_t)m1 * H + k2);
   __syncthreads();
   const cplx* res = line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
   unsigned long long emax = 0;
