@@ -84,6 +84,9 @@ double line_ops(const LinePlan& lp) {
 
 int padded_stride(int L) { return L + (L >> 4) + 1; }
 
+// FP64-instruction equivalent of one CTA's fixed cost in a batch launch
+constexpr double kBatchUnitOverhead = 2000.0;
+
 int stage_offsets(const LinePlan& lp, int* off);
 
 // Shared memory of a row-pass CTA: four line buffers (the pair, ping-pong) and the copy of
@@ -121,8 +124,15 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
     const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = row_smem(W, a);
     if (smc > (size_t)kMaxDynSmem || smr > (size_t)kMaxDynSmem) continue;
     if ((H + kElemsPerThread - 1) / kElemsPerThread > 4 * kMaxThreads) continue;
-    const double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
-    const double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * line_ops(a) + 16.0);
+    double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
+    double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * line_ops(a) + 16.0);
+    if (sms == 1) {
+      // a batch member: its units share the device with the batch's other units, so the
+      // fixed cost of a CTA (launch, descriptor copy, barriers, global round trips) is
+      // charged per unit, which keeps the lines long enough to amortise it
+      col += (double)W * kBatchUnitOverhead;
+      row += (double)(H / 2 + 1) * kBatchUnitOverhead;
+    }
     double cost = 2.0 * col + row;
     // prefer smaller shared-memory footprints (more resident CTAs) on ties
     cost *= 1.0 + 0.02 * (double)(smc + smr) / (64.0 * 1024);
