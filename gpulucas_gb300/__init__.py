@@ -162,6 +162,7 @@ def _load():
         "gl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
         "gl_version": (ctypes.c_int, []),
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+        "gl_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
         "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gl_smallest_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
@@ -219,7 +220,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
     "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query",
     "gl_server_default_opts", "gl_server_create", "gl_server_submit", "gl_server_poll", "gl_server_drain",
-    "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy",
+    "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy", "gl_selftest_bounded_wait",
 ]))
 
 

@@ -1062,6 +1062,23 @@ int mersenneTest(int testPrime, int signalSize) {
   return res.is_prime;
 }
 
+int gl_selftest_bounded_wait(int device, int tries) {
+  if (tries < 1) return GL_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GL_ERR_NODEVICE;
+  if (device < 0 || device >= ndev || cudaSetDevice(device) != cudaSuccess) return GL_ERR_ARG;
+  Status* d = nullptr;
+  Status h{};
+  if (cudaMalloc(&d, sizeof(Status)) != cudaSuccess) return GL_ERR_NOMEM;
+  int rc = GL_OK;
+  if (cudaMemset(d, 0, sizeof(Status)) != cudaSuccess || launch_wait_selftest(d, tries, 0) != cudaSuccess ||
+      cudaMemcpy(&h, d, sizeof(Status), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = GL_ERR_CUDA;
+  cudaFree(d);
+  if (rc != GL_OK) return rc;
+  return (h.flags & kStatusTimeout) ? GL_ERR_TIMEOUT : GL_OK;
+}
+
 int gl_probe_fp64_peak(int device, double ms, double* tflops) {
   if (!tflops || ms <= 0) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(device));

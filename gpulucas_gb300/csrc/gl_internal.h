@@ -109,6 +109,7 @@ constexpr int kResidentAutoN = 4096;   // used by default up to here: measured f
 // smallest cluster first; fills r and returns cudaSuccess if the layout fits one cluster
 cudaError_t resident_geom(const FusedGeom& g, int twH_n, int twW_n, int n, ResidentGeom* r);
 cudaError_t launch_resident(const IterArgs& a, const ResidentGeom& r, int iters, cudaStream_t s);
+cudaError_t launch_wait_selftest(Status* st, int tries, cudaStream_t s);
 
 // A batch of fused-form tests advanced by one set of launches: the descriptor table of
 // every test's arguments (device) and the unit maps (test, local column / row pair).

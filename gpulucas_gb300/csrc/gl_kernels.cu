@@ -69,8 +69,8 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < kWaitTries; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int tries = kWaitTries) {
+  for (int i = 0; i < tries; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -1015,4 +1015,20 @@ cudaError_t launch_resident(const IterArgs& a, const ResidentGeom& g, int iters,
   }
 }
 
+
+// Self-test of the bounded wait: an mbarrier that expects one arrival nobody makes.  The
+// wait gives up after `tries` polls, the block records kStatusTimeout exactly as the row
+// pass does, and the kernel returns; the context stays usable.
+__global__ void k_wait_selftest(Status* st, int tries) {
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar);
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0, tries);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(&st->flags, kStatusTimeout);
+}
+
+cudaError_t launch_wait_selftest(Status* st, int tries, cudaStream_t s) {
+  k_wait_selftest<<<1, 64, 0, s>>>(st, tries);
+  return cudaGetLastError();
+}
 }  // namespace gl

@@ -355,6 +355,10 @@ int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* ll_out, int6
 /* --- utilities ----------------------------------------------------------- */
 const char* gl_error_string(int status);
 int gl_version(void);        /* major*10000 + minor*100 + patch */
+/* Self-test of the kernels' bounded waits: a kernel waits on a barrier nothing completes,
+ * gives up after `tries` polls and reports it; returns GL_ERR_TIMEOUT when the timeout
+ * path works (the device stays usable), GL_OK if the wait unexpectedly completed. */
+int gl_selftest_bounded_wait(int device, int tries);
 /* FP64 throughput probe (DFMA), for the roofline denominator: TFLOP/s counting an FMA
  * as 2 flops, measured on `device` for about `ms` milliseconds. */
 int gl_probe_fp64_peak(int device, double ms, double* tflops);

@@ -189,6 +189,15 @@ def test_roundoff_abort_is_reported(gl):
         assert rep.iterations < 2000
 
 
+def test_bounded_wait_times_out_and_device_stays_usable(gl, orc):
+    """A kernel waiting on a barrier that nothing completes gives up after its bound,
+    the host reads GL_ERR_TIMEOUT, and the context keeps working (no trap, no hang)."""
+    assert gl.lib.gl_selftest_bounded_wait(0, 1000) == gl.GL_ERR_TIMEOUT
+    with gl.Plan(44497, 2048) as pl:
+        pl.iterate(100)
+        assert pl.res64() == orc.Exact(44497).iterate(100).res64()
+
+
 def test_plans_with_different_layouts_coexist(gl):
     """Two live plans of different layouts (autotuned and forced) interleave correctly."""
     p, N = 2976221, 163840
