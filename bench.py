@@ -369,7 +369,7 @@ def served_leg(gl, dev: int, window: int) -> dict:
     """The served configuration: the first `window` requests of the seeded Poisson stream
     (mean 50/s; 80% Res64 checks after 5000 iterations with p log-uniform in [1e5, 5e7],
     20% full tests with p log-uniform in [1e5, 2e6]), served in real time with continuous
-    batching against a 150 GB HBM budget, each test at gl_safe_signal_size's length.  The stream is far over one GPU's capacity, so
+    batching against a 150 GB HBM budget, each test at gl_fast_signal_size's length.  The stream is far over one GPU's capacity, so
     the window is finite and the server runs saturated until it drains.  Compared with
     the same requests run one at a time in arrival order (plain and fused form, from each
     form's measured ms/iteration at each N)."""
@@ -387,7 +387,8 @@ def served_leg(gl, dev: int, window: int) -> dict:
         "requests": window, "full_tests": sum(r.full for r in reqs),
         "errors": sum(1 for c in done if c.status != 0),
         "restarts_at_larger_length": sum(c.attempts - 1 for c in done),
-        "length_rule": "gl_safe_signal_size: p/N <= 19.2 - 0.26 log2(N/163840)",
+        "length_rule": "gl_fast_signal_size(p, 0.2): within 20 % above the length with "
+                       "p/N <= 19.2 - 0.26 log2(N/163840), odd part 1 or 3 preferred",
         "primes_found": [c.p for c in done if c.is_prime],
         "max_roundoff": max(c.max_roundoff for c in done),
         "tflops_alg": srv.stats["flop"] / srv.stats["wall_s"] / 1e12,

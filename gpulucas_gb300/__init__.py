@@ -167,6 +167,7 @@ def _load():
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gl_smallest_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
         "gl_safe_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        "gl_fast_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
         "gl_batch_create": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
         "gl_batch_create_from_plans": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PlanOpts), PP]),
         "gl_batch_query": (ctypes.c_int, [P]),
@@ -218,7 +219,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
     "gl_checkpoint_read", "gl_plan_resume", "gl_smallest_signal_size", "gl_batch_create", "gl_batch_destroy",
     "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
-    "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query",
+    "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query", "gl_fast_signal_size",
     "gl_server_default_opts", "gl_server_create", "gl_server_submit", "gl_server_poll", "gl_server_drain",
     "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy", "gl_selftest_bounded_wait",
 ]))
@@ -476,6 +477,13 @@ def safe_signal_size(p: int) -> int:
     """Smallest length whose word size keeps the measured round-off <= 0.125 (host only)."""
     N = ctypes.c_int()
     _check(lib.gl_safe_signal_size(int(p), ctypes.byref(N)), "safe_signal_size")
+    return N.value
+
+
+def fast_signal_size(p: int, slack: float = 0.2) -> int:
+    """Cheapest modelled length within (1 + slack) of safe_signal_size (host only)."""
+    N = ctypes.c_int()
+    _check(lib.gl_fast_signal_size(int(p), float(slack), ctypes.byref(N)), "fast_signal_size")
     return N.value
 
 

@@ -441,6 +441,11 @@ void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters) {
   pl->carry_valid = pl->mode == GL_MODE_PLAIN;
 }
 
+double gl_model_iteration_cost(int M, int sms) {
+  const auto r = ranked_layouts(M, sms);
+  return r.empty() ? HUGE_VAL : r.front().first;
+}
+
 double gl_plan_unit_cost(const gl_plan* pl, bool row) {
   if (row) return 2.0 * pl->fg.W * (2.0 * line_ops(pl->fg.pw) + 16.0);
   return pl->fg.H * (line_ops(pl->fg.ph) + 6.0);

@@ -45,5 +45,8 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
 void gl_plan_note_external_iterations(gl_plan* pl, int64_t iters);
 // non-blocking stream; level 0: normal priority, 1: the device's highest, 2: between
 cudaError_t gl_make_stream(cudaStream_t* s, int level);
+// modelled time of the best fused layout for M complex points on `sms` SMs (layout
+// cost model units), +inf if no layout exists
+double gl_model_iteration_cost(int M, int sms);
 // cost of one column-pass unit and one row-pass unit of a fused plan (FP64 model)
 double gl_plan_unit_cost(const gl_plan* pl, bool row);

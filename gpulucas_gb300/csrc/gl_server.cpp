@@ -61,7 +61,7 @@ gl_plan_opts engine_opts(const GpuEngine* g) {
 int ge_signal_size(void*, int p, double bits, int above, int* N) {
   if (above) return gl_smallest_signal_size(p, (double)p / (above + 1.0), N);
   if (bits > 0.0) return gl_smallest_signal_size(p, bits, N);
-  return gl_safe_signal_size(p, N);
+  return gl_fast_signal_size(p, 0.2, N);
 }
 int ge_footprint(void* ctx, int p, int N, size_t* bytes) {
   gl_plan_opts o = engine_opts(static_cast<GpuEngine*>(ctx));

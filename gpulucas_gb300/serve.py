@@ -15,7 +15,9 @@ S0 = 4 at the next larger FFT length (the reference aborts such a run,
 gpuLucas.cu:1470-1479).  Residues stay on the device; a finished test reports its Res64
 and zero test and frees its memory.
 
-This module drives that server from Python: `Server.run` submits a request list in real
+FFT lengths come from gl_fast_signal_size (within 20 % above the round-off-safe length,
+the fastest kind of length), or from a fixed bits/word bound when `max_bits_per_word` is
+given.  This module drives that server from Python: `Server.run` submits a request list in real
 time (each request at its arrival time) or all at once, and collects the completions.
 An engine object (see `PyEngine`) can stand in for the GPU so the scheduling logic runs
 on the CPU in the tests.  The reference runs one test per process (gpuLucas.cu:374-639)

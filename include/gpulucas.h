@@ -201,6 +201,11 @@ int gl_smallest_signal_size(int p, double max_bits_per_word, int* N_out);
  * the tail of long runs.  A host-only length rule for servers that cannot afford
  * gl_find_signal_size's trial runs. */
 int gl_safe_signal_size(int p, int* N_out);
+/* A fast length in [gl_safe_signal_size, (1 + slack) x that]: the smallest whose odd
+ * part is 1 or 3 (measured fastest: 98304 = 2^15 3 takes 33 us per iteration where
+ * 84672 = 2^6 3^3 7^2 takes 41 us), else the cheapest under the layout cost model.
+ * Host only. */
+int gl_fast_signal_size(int p, double slack, int* N_out);
 
 typedef struct gl_batch gl_batch;
 typedef struct {
@@ -261,7 +266,7 @@ typedef struct gl_server_opts {
     int max_active;              /* live tests at most */
     double step_ms;              /* GPU time per lane step at most */
     int64_t checkpoint_every;    /* Res64 of full tests every this many iterations (0: never) */
-    double max_bits_per_word;    /* > 0: smallest length with p/N <= this; else gl_safe_signal_size */
+    double max_bits_per_word;    /* > 0: smallest length with p/N <= this; else gl_fast_signal_size(p, 0.2) */
     int retries;                 /* restarts at a larger length after a round-off abort */
     int64_t chain_iterations;    /* requests longer than this go to the chain lane */
     int lanes;                   /* 3: lead + chain + bulk; 2: chain + bulk; 1: one batch */
