@@ -45,7 +45,8 @@ class PlanOpts(ctypes.Structure):
                 ("check_every", ctypes.c_int), ("use_graphs", ctypes.c_int), ("fft_h", ctypes.c_int),
                 ("cols_per_cta", ctypes.c_int), ("autotune", ctypes.c_int), ("batch_layout", ctypes.c_int),
                 ("high_priority", ctypes.c_int), ("max_radix_col", ctypes.c_int),
-                ("max_radix_row", ctypes.c_int), ("resident", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
+                ("max_radix_row", ctypes.c_int), ("resident", ctypes.c_int),
+                ("col_inplace", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
 
 
 class PlanInfo(ctypes.Structure):

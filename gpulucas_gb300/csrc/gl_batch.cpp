@@ -141,7 +141,8 @@ int assemble(gl_batch* b) {
     desc[i].status = b->d_status + i;
     t_col = std::max(t_col, b->plans[i]->fg.t_col);
     t_row = std::max(t_row, b->plans[i]->fg.t_row);
-    sm_col = std::max(sm_col, b->plans[i]->fg.sm_col);
+    // the batched column kernels always use the two-buffer line DFT
+    sm_col = std::max(sm_col, (size_t)2 * b->plans[i]->fg.ls_col * 16);
     sm_row = std::max(sm_row, b->plans[i]->fg.sm_row);
   }
   IterArgs* d_desc = nullptr;

@@ -145,7 +145,8 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
 // Layout for M: column length `force_h` (0: the model's best) with line plans whose
 // largest radix is rc (columns) / rr (rows); each line gets one thread per butterfly
 // of its largest-radix stage.
-int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix) {
+int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix,
+                      bool ip = false) {
   if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
   int bestH = 0;
   for (const auto& c : ranked_layouts(M, sms))
@@ -170,6 +171,18 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   };
   g->t_col = threads(g->H, rc, kMaxThreads);
   g->t_row = threads(2 * g->W, rr, kRowThreads);
+  g->col_ip = 0;
+  if (ip) {
+    // in place: every column stage has at most (8 / R for radix R = 2^k, 1 for odd R)
+    // butterflies per thread, held in registers across the stage's first barrier
+    for (int s = 0; s < g->ph.nst; ++s) {
+      const int R = g->ph.radix[s];
+      const int per = (R & (R - 1)) == 0 ? 8 / R : 1;
+      if (g->H / R > per * g->t_col) return GL_ERR_SIZE;
+    }
+    g->col_ip = 1;
+    g->sm_col = (size_t)g->ls_col * 16;
+  }
   return GL_OK;
 }
 
@@ -196,9 +209,9 @@ int stage_offsets(const LinePlan& lp, int* off) {
 
 // Device time of one fused iteration with column length H, measured on zero-filled
 // buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
-double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cudaStream_t s) {
+double time_layout(int M, int H, int rc, int rr, bool ip, int n, int sms, int iters, cudaStream_t s) {
   FusedGeom g{};
-  if (choose_fused_geom(M, H, sms, &g, rc, rr) != GL_OK) return -1.0;
+  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip) != GL_OK) return -1.0;
   const int N = 2 * M;
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
@@ -246,6 +259,7 @@ double time_layout(int M, int H, int rc, int rr, int n, int sms, int iters, cuda
 // radix-2 caps below 2^15).
 struct TunedLayout {
   int H = 0, rc = kMaxRadix, rr = kMaxRadix;
+  bool ip = false;
   double ms = 0.0;
 };
 std::mutex g_tune_mutex;
@@ -264,25 +278,30 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
   TunedLayout best;
   double best_ms = 1e300;
   const int iters = M >= (1 << 18) ? 10 : 40;
-  auto consider = [&](int H, int rc, int rr) {
-    const double ms = time_layout(M, H, rc, rr, n, sms, iters, s);
+  auto consider = [&](int H, int rc, int rr, bool ip) {
+    const double ms = time_layout(M, H, rc, rr, ip, n, sms, iters, s);
     if (ms > 0.0 && ms < best_ms) {
       best_ms = ms;
       best.H = H;
       best.rc = rc;
       best.rr = rr;
+      best.ip = ip;
     }
   };
-  for (size_t i = 0; i < ranked.size() && i < 6; ++i) consider(ranked[i].second, kMaxRadix, kMaxRadix);
+  for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
+    consider(ranked[i].second, kMaxRadix, kMaxRadix, false);
+    // long columns: the in-place column passes (half the shared memory, 4 CTAs per SM)
+    if (M >= (1 << 17)) consider(ranked[i].second, kMaxRadix, kMaxRadix, true);
+  }
   if (M < (1 << 17))
     for (size_t i = 0; i < ranked.size() && i < 3; ++i) {
-      consider(ranked[i].second, 4, kMaxRadix);
-      consider(ranked[i].second, kMaxRadix, 4);
-      consider(ranked[i].second, 4, 4);
+      consider(ranked[i].second, 4, kMaxRadix, false);
+      consider(ranked[i].second, kMaxRadix, 4, false);
+      consider(ranked[i].second, 4, 4, false);
       if (M < (1 << 15)) {  // lines of at most a few hundred points: radix-2 stages too
-        consider(ranked[i].second, 2, 4);
-        consider(ranked[i].second, 4, 2);
-        consider(ranked[i].second, 2, 2);
+        consider(ranked[i].second, 2, 4, false);
+        consider(ranked[i].second, 4, 2, false);
+        consider(ranked[i].second, 2, 2, false);
       }
     }
   if (!best.H) return best;
@@ -505,16 +524,21 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     cudaGetLastError();
   }
   if (o.resident > 0 && !resident) return GL_ERR_SIZE;
+  bool col_ip = false;
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
       force_h = t.H;
       if (!o.max_radix_col) cap_c = t.rc;
       if (!o.max_radix_row) cap_r = t.rr;
+      col_ip = t.ip && !resident;
     }
   }
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r)
+  if (o.col_inplace) col_ip = o.col_inplace > 0 && !resident && !sms_override;
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip)
                                    : choose_plain_geom(M, &pg);
+  if (rc == GL_ERR_SIZE && col_ip && o.col_inplace <= 0)  // the searched layout cannot: two buffers
+    rc = choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, false);
   if (rc != GL_OK) return rc;
 
   gl_plan* pl = new (std::nothrow) gl_plan();

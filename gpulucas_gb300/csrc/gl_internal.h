@@ -47,6 +47,7 @@ constexpr unsigned kStatusTimeout = 4u; // a bounded device-side wait ran out (k
 // is stored column-major: word j = 2(m1 + W m2) + e lives at 2(m1 H + m2) + e.
 struct FusedGeom {
   int W, H, G;
+  int col_ip;                // column passes run their DFTs in place (one buffer, 4 CTAs/SM)
   int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
                              // a smaller cap means more, shorter butterflies per stage and
                              // so more threads per line, for lengths too short to fill the GPU

@@ -161,6 +161,91 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
   return a;
 }
 
+// In-place variant (one buffer, two barriers per stage): every thread first reads the
+// inputs of all its butterflies of the stage into registers (at most 8 points: one radix-8
+// butterfly, two radix-4, four radix-2, one odd-radix), then, after the barrier, computes
+// and writes them back.  Half the shared memory of the ping-pong form, so more CTAs fit
+// on an SM; usable when every stage has at most that many butterflies per thread.
+template <int R>
+__host__ __device__ constexpr int ip_butterflies() {
+  return (R & (R - 1)) == 0 ? 8 / R : 1;
+}
+
+template <int R, int S, typename TW>
+__device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nlines, int ls, int L, int Ns,
+                                                  const TW* __restrict__ tw) {
+  constexpr bool POW2 = (R & (R - 1)) == 0;
+  constexpr int NV = POW2 ? (R == 2 ? 1 : R / 2) : R - 1;
+  constexpr int B = ip_butterflies<R>();
+  const int LR = L / R;
+  const int nb = nlines * LR;
+  cplx held[B * R];
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    const int b = threadIdx.x + i * blockDim.x;
+    const int bb = b < nb ? b : 0;  // a thread without this butterfly reads a valid slot
+    const int l = bb / LR;
+    const int j = bb - l * LR;
+    const cplx* s = buf + l * ls;
+#pragma unroll
+    for (int q = 0; q < R; ++q) held[i * R + q] = s[pad(j + q * LR)];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    const int b = threadIdx.x + i * blockDim.x;
+    if (b < nb) {
+      const int l = b / LR;
+      const int j = b - l * LR;
+      const int k = j % Ns;
+      cplx v[R];
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = held[i * R + q];
+      if (Ns > 1) {
+        cplx tv[NV];
+#pragma unroll
+        for (int t = 0; t < NV; ++t) {
+          const cplx w = tw_at(tw + (size_t)t * Ns + k);
+          tv[t] = S < 0 ? w : conj(w);
+        }
+        if constexpr (POW2) {
+          layered_dit<R, S, true>(v, tv);
+        } else {
+#pragma unroll
+          for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tv[q - 1]);
+          dft<R, S>(v);
+        }
+      } else {
+        if constexpr (POW2) layered_dit<R, S, false>(v, nullptr);
+        else dft<R, S>(v);
+      }
+      cplx* d = buf + l * ls;
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) d[pad(base + q * Ns)] = v[q];
+    }
+  }
+  __syncthreads();
+}
+
+template <int S, typename TW>
+__device__ __forceinline__ cplx* line_fft_ip(cplx* a, int nlines, int ls, const LinePlan& lp, const TW* tw) {
+  int Ns = 1;
+  for (int s = 0; s < lp.nst; ++s) {
+    const TW* st = tw + lp.off[s];
+    switch (lp.radix[s]) {
+      case 8: stockham_stage_ip<8, S>(a, nlines, ls, lp.L, Ns, st); break;
+      case 4: stockham_stage_ip<4, S>(a, nlines, ls, lp.L, Ns, st); break;
+      case 2: stockham_stage_ip<2, S>(a, nlines, ls, lp.L, Ns, st); break;
+      case 3: stockham_stage_ip<3, S>(a, nlines, ls, lp.L, Ns, st); break;
+      case 5: stockham_stage_ip<5, S>(a, nlines, ls, lp.L, Ns, st); break;
+      default: stockham_stage_ip<7, S>(a, nlines, ls, lp.L, Ns, st); break;
+    }
+    Ns *= lp.radix[s];
+  }
+  return a;
+}
+
 // Real-signal split and square for one frequency pair (k, M-k).  With U the DFT of
 // u[m] = x[2m] + i x[2m+1], E/O the DFTs of the even/odd words, E + iO = U_k, so the
 // DFT of (z_even + i z_odd) of the squared signal is
@@ -190,7 +275,7 @@ __device__ __forceinline__ int colmajor(const IterArgs& a, int j) {
 // Column pass, forward.  NC = carry depth n of llintToIrrBal<n>.  For words
 // j0 = 2m, j0+1 the digit sums of j0-1, j0, j0+1 need the products of words
 // j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.
-template <bool FROM_STATE, int NC>
+template <bool FROM_STATE, int NC, bool IP = false>
 __device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
   extern __shared__ cplx smem[];
   const int H = a.H, W = a.W, N = a.N;
@@ -248,15 +333,16 @@ __device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
     smem[pad(m2)] = mk(A.x * dbl_from_int(v0), A.y * dbl_from_int(v1));
   }
   __syncthreads();
-  const cplx* res = line_fft<-1>(smem, buf1, 1, ls, a.ph, a.twH);
+  const cplx* res = IP ? line_fft_ip<-1>(smem, 1, ls, a.ph, a.twH) : line_fft<-1>(smem, buf1, 1, ls, a.ph, a.twH);
   const DevCplx* tw = a.twK1 + (size_t)m1 * H;
   for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x)
     st(a.Z + (size_t)k2 * W + m1, cmul(res[pad(k2)], ld(tw + k2)));
 }
 
-template <bool FROM_STATE, int NC>
-__global__ void __launch_bounds__(kMaxThreads, 3) k_col_fwd(IterArgs a) {
-  col_fwd_body<FROM_STATE, NC>(a, blockIdx.x);
+// IP: the in-place line DFT, half the shared memory, four CTAs per SM
+template <bool FROM_STATE, int NC, bool IP>
+__global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 3) k_col_fwd(IterArgs a) {
+  col_fwd_body<FROM_STATE, NC, IP>(a, blockIdx.x);
 }
 
 // The row pass's stage twiddles (a few KB) are copied into shared memory behind the four
@@ -368,6 +454,7 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
   return r;
 }
 
+template <bool IP = false>
 __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   extern __shared__ cplx smem[];
   const int H = a.H;
@@ -375,7 +462,7 @@ __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   cplx* buf1 = smem + ls;
   for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z2 + (size_t)m1 * H + k2);
   __syncthreads();
-  const cplx* res = line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
+  const cplx* res = IP ? line_fft_ip<+1>(smem, 1, ls, a.ph, a.twH) : line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
   unsigned long long emax = 0;
   unsigned fl = 0;
   for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
@@ -391,7 +478,10 @@ __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   finish_status(a, emax, fl);
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 3) k_col_inv(IterArgs a) { col_inv_body(a, blockIdx.x); }
+template <bool IP>
+__global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 3) k_col_inv(IterArgs a) {
+  col_inv_body<IP>(a, blockIdx.x);
+}
 
 // ---------------------------------------------------------------------------
 // Batched kernels: many tests advance together.  units[blockIdx.x] = (test, local
@@ -435,7 +525,7 @@ __global__ void __launch_bounds__(kMaxThreads, 3) kb_col_inv(const IterArgs* __r
   __shared__ IterArgs sa;
   const int2 u = units[blockIdx.x];
   load_desc(tests, u.x, sa);
-  col_inv_body(sa, u.y);
+  col_inv_body<false>(sa, u.y);
 }
 
 cudaError_t set_batch_smem_limits() {
@@ -454,14 +544,14 @@ cudaError_t launch_batch_iteration(const BatchLaunch& b, cudaStream_t s, bool fr
   return cudaGetLastError();
 }
 
-template <bool FS>
+template <bool FS, bool IP>
 static cudaError_t set_col_fwd_smem(int bytes) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
-  return cudaFuncSetAttribute(k_col_fwd<FS, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 2, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 3, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 4, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd<FS, 5, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  return cudaFuncSetAttribute(k_col_fwd<FS, 6, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 // The attribute is per kernel and process-wide, shared by every plan: it is raised to the
@@ -469,35 +559,49 @@ static cudaError_t set_col_fwd_smem(int bytes) {
 cudaError_t set_fused_smem_limits(const FusedGeom& g) {
   if (g.sm_col > (size_t)kMaxDynSmem || g.sm_row > (size_t)kMaxDynSmem) return cudaErrorInvalidValue;
   cudaError_t e;
-  if ((e = set_col_fwd_smem<false>(kMaxDynSmem))) return e;
-  if ((e = set_col_fwd_smem<true>(kMaxDynSmem))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_smem<false, false>(kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_smem<true, false>(kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_smem<false, true>(kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_smem<true, true>(kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
   return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+}
+
+template <bool FS, bool IP>
+static void launch_col_fwd_ip(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
+  switch (a.n) {
+    case 2: k_col_fwd<FS, 2, IP><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 3: k_col_fwd<FS, 3, IP><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 4: k_col_fwd<FS, 4, IP><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    case 5: k_col_fwd<FS, 5, IP><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+    default: k_col_fwd<FS, 6, IP><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
+  }
 }
 
 template <bool FS>
 static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  switch (a.n) {
-    case 2: k_col_fwd<FS, 2><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
-    case 3: k_col_fwd<FS, 3><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
-    case 4: k_col_fwd<FS, 4><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
-    case 5: k_col_fwd<FS, 5><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
-    default: k_col_fwd<FS, 6><<<a.W, g.t_col, g.sm_col, s>>>(a); break;
-  }
+  if (g.col_ip) launch_col_fwd_ip<FS, true>(a, g, s);
+  else launch_col_fwd_ip<FS, false>(a, g, s);
+}
+
+static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
+  if (g.col_ip) k_col_inv<true><<<a.W, g.t_col, g.sm_col, s>>>(a);
+  else k_col_inv<false><<<a.W, g.t_col, g.sm_col, s>>>(a);
 }
 
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state) {
   if (from_state) launch_col_fwd<true>(a, g, s);
   else launch_col_fwd<false>(a, g, s);
   k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
-  k_col_inv<<<a.W, g.t_col, g.sm_col, s>>>(a);
+  launch_col_inv(a, g, s);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fused_kernel(const IterArgs& a, const FusedGeom& g, cudaStream_t s, int which) {
   if (which == 0) launch_col_fwd<false>(a, g, s);
   else if (which == 1) k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
-  else k_col_inv<<<a.W, g.t_col, g.sm_col, s>>>(a);
+  else launch_col_inv(a, g, s);
   return cudaGetLastError();
 }
 

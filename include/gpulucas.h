@@ -64,7 +64,9 @@ typedef struct {
                               thread-block cluster holding the test in shared memory;
                               0 = by default up to N = 4096 (where it is faster),
                               1 = require (N <= 32768), -1 = never */
-    int reserved[2];
+    int col_inplace;       /* fused form: column passes with in-place line DFTs (one buffer,
+                              four CTAs per SM); 0 = the autotuner decides, 1 = use, -1 = never */
+    int reserved[1];
 } gl_plan_opts;
 
 typedef struct {

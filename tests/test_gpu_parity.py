@@ -113,6 +113,23 @@ def test_resident_form_matches_oracle(gl, orc, p, N):
         assert pl.res64() == orc.Exact(p).iterate(63).res64()
 
 
+@pytest.mark.parametrize("p,N,H", [(2976221, 163840, 256), (20000000, 1179648, 2048), (43112609, 2359296, 2048),
+                                   (43112609, 2359296, 1024)])
+def test_inplace_column_passes_match(gl, orc, p, N, H):
+    """The in-place column DFTs (one shared-memory buffer, four CTAs per SM; power-of-two
+    column lengths) give the products of the two-buffer form, and the oracle's."""
+    with gl.Plan(p, N, col_inplace=1, fft_h=H, autotune=0) as a, \
+            gl.Plan(p, N, col_inplace=-1, fft_h=H, autotune=0) as b:
+        assert a.info.smem_col * 2 - 16 <= b.info.smem_col <= a.info.smem_col * 2 + 16
+        a.iterate(7)
+        b.iterate(7)
+        pa = a.products()
+        assert (pa == b.products()).all()
+        if N <= 163840:
+            o = orc.IBDWT(p, N).iterate(7)
+            assert (pa == o.ll()).all()
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432), (2976221, 163840)])
 @pytest.mark.parametrize("caps", [(4, 4), (2, 2), (4, 8), (8, 2)])
 def test_radix_capped_layouts_match_oracle(gl, orc, p, N, caps):
