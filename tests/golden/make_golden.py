@@ -1,12 +1,15 @@
 """Generate the committed golden fixtures under tests/golden/.
 
-Run in a container with mpmath:  python tests/golden/make_golden.py [--quick]
+Run in a container with mpmath:  python tests/golden/make_golden.py [--quick | --batch]
 
 * weights.json  -- IBDWT weights A[j] = 2^(ceil(jp/N) - jp/N) and Ainv[j] = (1/A[j])/N
   (computeWeightVectors, gpuLucas.cu:673-686) correctly rounded from 140-bit mpmath, at
   sampled j for the configured (p, N).
 * twiddles.json -- exp(-2 pi i t/L) correctly rounded (mpmath cospi/sinpi).
-* res64.json    -- Res64 of S_k mod 2^p - 1 (S_0 = 4) for (p, N, k).  Each entry is
+* res64.json    -- Res64 of S_k mod 2^p - 1 (S_0 = 4) for (p, N, k).
+* res64_batch.json -- the same for six of the batched configuration's 256 seeded
+  exponents (workloads.batch_exponents) at its length rule (smallest 7-smooth even N with
+  p/N <= 19.5) after its 10000 iterations.  Each entry is
   computed twice, by the exact NTT oracle (exact_oracle.c) and by the IBDWT oracle
   (ibdwt_oracle.c, the reference algorithm restated), and kept only when they agree.
   Entries with k = p - 2 for Mersenne-prime exponents must be 0.
@@ -96,7 +99,30 @@ def res64_entry(p: int, N: int, k: int, threads: int = 0):
             "oracle_maxerr": round(err, 6)}
 
 
+def batch_fixture(threads: int = 0):
+    import gpulucas_gb300 as gl
+    from gpulucas_gb300 import workloads
+    ps = sorted(workloads.batch_exponents())
+    path = os.path.join(HERE, "res64_batch.json")
+    entries = []
+    if os.path.exists(path):
+        with open(path) as f:
+            entries = json.load(f)
+    have = {e["p"] for e in entries}
+    for i in (0, 1, 50, 128, 200, 255):
+        p = ps[i]
+        if p in have:
+            continue
+        entries.append(res64_entry(p, gl.smallest_signal_size(p, 19.5), 10000, threads))
+        with open(path, "w") as f:
+            json.dump(entries, f, indent=1)
+
+
 def main():
+    if "--batch" in sys.argv:
+        oracle.build()
+        batch_fixture()
+        return
     quick = "--quick" in sys.argv
     oracle.build()
     with open(os.path.join(HERE, "weights.json"), "w") as f:
