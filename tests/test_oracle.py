@@ -146,3 +146,18 @@ def test_golden_res64_fixture_consistent():
     for e in entries:
         if e["k"] == e["p"] - 2 and e["p"] in (44497, 86243, 2976221, 43112609):
             assert e["is_zero"] and int(e["res64"], 16) == 0
+
+
+def test_batch_golden_small_entries_recomputed():
+    """The batched configuration's golden Res64 (k = 10000), recomputed for the two small
+    exponents by the exact oracle."""
+    import json
+    import os
+
+    import oracle
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "res64_batch.json")) as f:
+        entries = json.load(f)
+    assert len(entries) == 6 and all(e["k"] == 10000 for e in entries)
+    for e in entries:
+        if e["p"] < 200000:
+            assert f"{oracle.Exact(e['p']).iterate(10000).res64():016x}" == e["res64"]
