@@ -4,8 +4,8 @@
 Default workload: one LL iteration of the large single test p = 43112609 at
 N = 2359296 = 2^18 * 3^2 (18.27 bits/word), the length the reference quotes its own
 iteration rate at (gpuLucas.cu:92-97).  A step is one iteration; the L2 cache is
-flushed (512 MiB write) before every timed step, because the test's whole working set
-(about 110 MB) would otherwise stay L2-resident.
+flushed (512 MiB write) before every timed step (the test's state and tables, about
+170 MB, exceed the 129 MB L2, but part of them would otherwise stay resident).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -293,7 +293,8 @@ def run_ours(args, world: int, rank: int, local: int):
         "data": "synthetic: the LL sequence from S0=4 (no dataset)",
         "config": {"workload": WORKLOAD,
                    "p": P3, "N": N3, "fft": f"{info.fft_h} x {info.fft_w}", "parallelism": "replicas",
-                   "l2": "flushed before every timed step (512 MiB write); working set ~110 MB < L2",
+                   "l2": "flushed before every timed step (512 MiB write); the test's ~170 MB of state and "
+                         "tables exceed the 129 MB L2 anyway",
                    "vs_baseline_note": "reference's published 204.72 iter/s at N=2359296 (GTX 480/C2050)"},
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": read_traffic(dom),
