@@ -255,8 +255,8 @@ double time_layout(int M, int H, int rc, int rr, bool ip, int n, int sms, int it
 // Autotuned layout for M on this device: the cheapest few column lengths of the cost
 // model are timed and the fastest kept, once per (M, SM count) per process.  Below
 // 2^17 complex points the lines are too short to fill the GPU with one thread per
-// radix-8 butterfly, so the three best lengths are also timed with radix-4 caps (and
-// radix-2 caps below 2^15).
+// radix-8 butterfly, so the three best lengths are also timed with radix-4 and radix-2
+// caps.
 struct TunedLayout {
   int H = 0, rc = kMaxRadix, rr = kMaxRadix;
   bool ip = false;
@@ -298,11 +298,11 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
       consider(ranked[i].second, 4, kMaxRadix, false);
       consider(ranked[i].second, kMaxRadix, 4, false);
       consider(ranked[i].second, 4, 4, false);
-      if (M < (1 << 15)) {  // lines of at most a few hundred points: radix-2 stages too
-        consider(ranked[i].second, 2, 4, false);
-        consider(ranked[i].second, 4, 2, false);
-        consider(ranked[i].second, 2, 2, false);
-      }
+      // radix-2 stages: the same FP64 work per point and bit in the layered form, twice
+      // the butterflies per stage, so twice the warps to hide FP64 latency on short lines
+      consider(ranked[i].second, 2, 4, false);
+      consider(ranked[i].second, 4, 2, false);
+      consider(ranked[i].second, 2, 2, false);
     }
   if (!best.H) return best;
   best.ms = best_ms;
