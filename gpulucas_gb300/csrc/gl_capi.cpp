@@ -146,7 +146,7 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
 // largest radix is rc (columns) / rr (rows); each line gets one thread per butterfly
 // of its largest-radix stage.
 int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix,
-                      bool ip = false) {
+                      bool ip = false, bool pf = false) {
   if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
   int bestH = 0;
   for (const auto& c : ranked_layouts(M, sms))
@@ -172,6 +172,7 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   g->t_col = threads(g->H, rc, kMaxThreads);
   g->t_row = threads(2 * g->W, rr, kRowThreads);
   g->col_ip = 0;
+  g->col_pf = 0;
   if (ip) {
     // in place: every column stage has at most (8 / R for radix R = 2^k, 1 for odd R)
     // butterflies per thread, held in registers across the stage's first barrier
@@ -182,6 +183,11 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
     }
     g->col_ip = 1;
     g->sm_col = (size_t)g->ls_col * 16;
+    if (pf) {
+      if (g->H % 8) return GL_ERR_SIZE;  // bulk copies of 2H bytes must be 16-byte multiples
+      g->col_pf = 1;
+      g->sm_col += (size_t)18 * g->H;
+    }
   }
   return GL_OK;
 }
@@ -209,9 +215,9 @@ int stage_offsets(const LinePlan& lp, int* off) {
 
 // Device time of one fused iteration with column length H, measured on zero-filled
 // buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
-double time_layout(int M, int H, int rc, int rr, bool ip, int n, int sms, int iters, cudaStream_t s) {
+double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, int n, int sms, int iters, cudaStream_t s) {
   FusedGeom g{};
-  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip) != GL_OK) return -1.0;
+  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip, pf) != GL_OK) return -1.0;
   const int N = 2 * M;
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
@@ -259,7 +265,7 @@ double time_layout(int M, int H, int rc, int rr, bool ip, int n, int sms, int it
 // caps.
 struct TunedLayout {
   int H = 0, rc = kMaxRadix, rr = kMaxRadix;
-  bool ip = false;
+  bool ip = false, pf = false;
   double ms = 0.0;
 };
 std::mutex g_tune_mutex;
@@ -278,20 +284,24 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
   TunedLayout best;
   double best_ms = 1e300;
   const int iters = M >= (1 << 18) ? 10 : 40;
-  auto consider = [&](int H, int rc, int rr, bool ip) {
-    const double ms = time_layout(M, H, rc, rr, ip, n, sms, iters, s);
+  auto consider = [&](int H, int rc, int rr, bool ip, bool pf = false) {
+    const double ms = time_layout(M, H, rc, rr, ip, pf, n, sms, iters, s);
     if (ms > 0.0 && ms < best_ms) {
       best_ms = ms;
       best.H = H;
       best.rc = rc;
       best.rr = rr;
       best.ip = ip;
+      best.pf = pf;
     }
   };
   for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
     consider(ranked[i].second, kMaxRadix, kMaxRadix, false);
     // long columns: the in-place column passes (half the shared memory, 4 CTAs per SM)
-    if (M >= (1 << 17)) consider(ranked[i].second, kMaxRadix, kMaxRadix, true);
+    if (M >= (1 << 17)) {
+      consider(ranked[i].second, kMaxRadix, kMaxRadix, true);
+      consider(ranked[i].second, kMaxRadix, kMaxRadix, true, true);
+    }
   }
   if (M < (1 << 17))
     for (size_t i = 0; i < ranked.size() && i < 3; ++i) {
@@ -524,7 +534,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     cudaGetLastError();
   }
   if (o.resident > 0 && !resident) return GL_ERR_SIZE;
-  bool col_ip = false;
+  bool col_ip = false, col_pf = false;
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
@@ -532,10 +542,14 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
       if (!o.max_radix_col) cap_c = t.rc;
       if (!o.max_radix_row) cap_r = t.rr;
       col_ip = t.ip && !resident;
+      col_pf = col_ip && t.pf;
     }
   }
-  if (o.col_inplace) col_ip = o.col_inplace > 0 && !resident && !sms_override;
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip)
+  if (o.col_inplace) {
+    col_ip = o.col_inplace > 0 && !resident && !sms_override;
+    col_pf = col_ip && o.col_inplace == 2;
+  }
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf)
                                    : choose_plain_geom(M, &pg);
   if (rc == GL_ERR_SIZE && col_ip && o.col_inplace <= 0)  // the searched layout cannot: two buffers
     rc = choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, false);

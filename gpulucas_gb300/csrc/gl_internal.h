@@ -48,6 +48,8 @@ constexpr unsigned kStatusTimeout = 4u; // a bounded device-side wait ran out (k
 struct FusedGeom {
   int W, H, G;
   int col_ip;                // column passes run their DFTs in place (one buffer, 4 CTAs/SM)
+  int col_pf;                // with col_ip: the inverse column pass bulk-copies its weights
+                             // and spans into shared memory (18 H bytes more)
   int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
                              // a smaller cap means more, shorter butterflies per stage and
                              // so more threads per line, for lengths too short to fill the GPU

@@ -53,8 +53,8 @@ constexpr int kWaitTries = 1 << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t arrivals = 1) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(arrivals) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
@@ -454,22 +454,50 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
   return r;
 }
 
-template <bool IP = false>
+// PF (with IP, H a multiple of 8): the column's inverse weights and spans (18 H bytes,
+// contiguous in the column-major tables) are brought into shared memory behind the line
+// buffer by two bulk copies issued at the start, so the rounding loop after the DFT does
+// not wait on global loads.
+template <bool IP = false, bool PF = false>
 __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
+  static_assert(!PF || IP, "the prefetch area follows the single in-place line buffer");
   extern __shared__ cplx smem[];
+  __shared__ alignas(8) uint64_t pf_bar;
   const int H = a.H;
   const int ls = a.ls_col;
   cplx* buf1 = smem + ls;
+  double* ai_s = reinterpret_cast<double*>(smem + ls);
+  unsigned char* sp_s = reinterpret_cast<unsigned char*>(ai_s + 2 * H);
+  if (PF) {
+    if (threadIdx.x == 0) mbar_init(&pf_bar, 2);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_load(ai_s, a.Ainv + (size_t)2 * m1 * H, 16u * (uint32_t)H, &pf_bar);
+      bulk_load(sp_s, a.span + (size_t)2 * m1 * H, 2u * (uint32_t)H, &pf_bar);
+    }
+  }
   for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z2 + (size_t)m1 * H + k2);
   __syncthreads();
   const cplx* res = IP ? line_fft_ip<+1>(smem, 1, ls, a.ph, a.twH) : line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
+  if (PF) {
+    const bool ok = mbar_wait(&pf_bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&a.status->flags, kStatusTimeout);
+        mbar_wait(&pf_bar, 0);  // the copies may still land in this CTA's shared memory
+      }
+      return;
+    }
+  }
   unsigned long long emax = 0;
   unsigned fl = 0;
   for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
     const int s0 = 2 * (m1 * H + m2);
     const cplx v = res[pad(m2)];
-    const double2 ai = __ldg(reinterpret_cast<const double2*>(a.Ainv + s0));
-    const uchar2 sp = __ldg(reinterpret_cast<const uchar2*>(a.span + s0));
+    const double2 ai = PF ? make_double2(ai_s[2 * m2], ai_s[2 * m2 + 1])
+                          : __ldg(reinterpret_cast<const double2*>(a.Ainv + s0));
+    const uchar2 sp = PF ? make_uchar2(sp_s[2 * m2], sp_s[2 * m2 + 1])
+                         : __ldg(reinterpret_cast<const uchar2*>(a.span + s0));
     long long r0 = round_word(v.re * ai.x, sp.x, &emax, &fl);
     const long long r1 = round_word(v.im * ai.y, sp.y, &emax, &fl);
     if (s0 == 0) r0 -= 2;  // word 0: the -2 of the LL step, exact on the rounded integer
@@ -478,9 +506,9 @@ __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   finish_status(a, emax, fl);
 }
 
-template <bool IP>
-__global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 3) k_col_inv(IterArgs a) {
-  col_inv_body<IP>(a, blockIdx.x);
+template <bool IP, bool PF>
+__global__ void __launch_bounds__(kMaxThreads, IP && !PF ? 4 : 3) k_col_inv(IterArgs a) {
+  col_inv_body<IP, PF>(a, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -563,8 +591,12 @@ cudaError_t set_fused_smem_limits(const FusedGeom& g) {
   if ((e = set_col_fwd_smem<true, false>(kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<false, true>(kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<true, true>(kMaxDynSmem))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_inv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
-  if ((e = cudaFuncSetAttribute(k_col_inv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
+    return e;
   return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
 }
 
@@ -586,8 +618,9 @@ static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s
 }
 
 static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  if (g.col_ip) k_col_inv<true><<<a.W, g.t_col, g.sm_col, s>>>(a);
-  else k_col_inv<false><<<a.W, g.t_col, g.sm_col, s>>>(a);
+  if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_col, s>>>(a);
+  else if (g.col_ip) k_col_inv<true, false><<<a.W, g.t_col, g.sm_col, s>>>(a);
+  else k_col_inv<false, false><<<a.W, g.t_col, g.sm_col, s>>>(a);
 }
 
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state) {

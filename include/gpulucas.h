@@ -65,7 +65,8 @@ typedef struct {
                               0 = by default up to N = 4096 (where it is faster),
                               1 = require (N <= 32768), -1 = never */
     int col_inplace;       /* fused form: column passes with in-place line DFTs (one buffer,
-                              four CTAs per SM); 0 = the autotuner decides, 1 = use, -1 = never */
+                              four CTAs per SM); 2: also bulk-copy the inverse pass's weights
+                              into shared memory; 0 = the autotuner decides, -1 = never */
     int reserved[1];
 } gl_plan_opts;
 

@@ -115,12 +115,15 @@ def test_resident_form_matches_oracle(gl, orc, p, N):
 
 @pytest.mark.parametrize("p,N,H", [(2976221, 163840, 256), (20000000, 1179648, 2048), (43112609, 2359296, 2048),
                                    (43112609, 2359296, 1024)])
-def test_inplace_column_passes_match(gl, orc, p, N, H):
+@pytest.mark.parametrize("mode", [1, 2], ids=["inplace", "inplace+prefetch"])
+def test_inplace_column_passes_match(gl, orc, p, N, H, mode):
     """The in-place column DFTs (one shared-memory buffer, four CTAs per SM; power-of-two
-    column lengths) give the products of the two-buffer form, and the oracle's."""
-    with gl.Plan(p, N, col_inplace=1, fft_h=H, autotune=0) as a, \
+    column lengths), with or without the bulk-copied inverse weights, give the products of
+    the two-buffer form, and the oracle's."""
+    with gl.Plan(p, N, col_inplace=mode, fft_h=H, autotune=0) as a, \
             gl.Plan(p, N, col_inplace=-1, fft_h=H, autotune=0) as b:
-        assert a.info.smem_col * 2 - 16 <= b.info.smem_col <= a.info.smem_col * 2 + 16
+        extra = 18 * H if mode == 2 else 0
+        assert b.info.smem_col == 2 * (a.info.smem_col - extra)
         a.iterate(7)
         b.iterate(7)
         pa = a.products()
