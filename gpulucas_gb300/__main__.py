@@ -1,7 +1,7 @@
 """Command line with the reference's flags (gpuLucas.cu:374-454):
 
     python -m gpulucas_gb300 [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain]
-                             [-H h] [p]
+                             [-H h] [-I mode] [p]
 
 -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); without -f the length is chosen as
         findSignalSize does (gpuLucas.cu:1064-1187)
@@ -12,6 +12,8 @@
 -k k    stop after k iterations and print Res64 (0 = full p-2 test)
 -m      execution form: fused (default) or plain
 -H h    fused form: FFT column length h (M = h x w), instead of the timed layout search
+-I mode fused form, with -H: column passes 1 in place, 2 in place + prefetched weights,
+        -1 two-buffer (the layout search picks among these otherwise)
 SIGINT / SIGTERM write a checkpoint and exit (gpuLucas.cu:365-369, 1425-1429).
 A full test appends the reference's result line to results.txt (gpuLucas.cu:1514-1548)
 and removes its checkpoint files (gpuLucas.cu:628-632).
@@ -44,6 +46,7 @@ def main(argv=None) -> int:
     ap.add_argument("-k", type=int, default=0)
     ap.add_argument("-m", choices=["fused", "plain"], default="fused")
     ap.add_argument("-H", type=int, default=0)
+    ap.add_argument("-I", type=int, default=0, choices=[-1, 0, 1, 2])
     ap.add_argument("p", nargs="?", type=int, default=0)
     a = ap.parse_args(argv)
     if a.h:
@@ -77,7 +80,7 @@ def main(argv=None) -> int:
     signal.signal(signal.SIGINT, _on_signal)
     signal.signal(signal.SIGTERM, _on_signal)
     t0 = time.time()
-    with gl.Plan(p, N, mode=mode, device=a.d, fft_h=a.H) as pl:
+    with gl.Plan(p, N, mode=mode, device=a.d, fft_h=a.H, col_inplace=a.I) as pl:
         i = pl.info
         if resume_k is not None:
             pl.resume(chk)

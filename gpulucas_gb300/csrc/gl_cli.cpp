@@ -1,11 +1,12 @@
 // gl_cli.cpp -- the `gpulucas` executable: the reference's command line over the C ABI.
 //
-//   gpulucas [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] [-H h] [p]
+//   gpulucas [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] [-H h] [-I mode] [p]
 //
 // Flags follow gpuLucas.cu:374-454: -f FFT length, -n exponent (or positional), -d CUDA
 // device, -c checkpoint frequency (iterations) to <p>.chk in the reference's format
 // (gpuLucas.cu:1414-1423, 1569-1665); -v verbose, -q quiet.  Added: -k stop after k
-// iterations and print Res64, -m execution form, -H column length of the fused layout.
+// iterations and print Res64, -m execution form, -H column length of the fused layout,
+// -I column-pass variant (1 in place, 2 in place + prefetched weights, -1 two buffers).
 // Without -f the length is chosen as findSignalSize does (gpuLucas.cu:1064-1187).  A run
 // that finds <p>.chk (or <p>.chk.bak) resumes from it.  SIGINT / SIGTERM write a
 // checkpoint and exit (gpuLucas.cu:365-369, 1425-1429).  A full test appends the result
@@ -28,7 +29,7 @@ void on_signal(int) { g_stop = 1; }
 void usage() {
   std::fprintf(stderr,
                "usage: gpulucas [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] "
-               "[-H h] [p]\n"
+               "[-H h] [-I mode] [p]\n"
                "  -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); default: timed search\n"
                "  -n p    exponent of 2^p - 1 (or give it as the last argument)\n"
                "  -d dev  CUDA device\n"
@@ -36,6 +37,7 @@ void usage() {
                "  -k k    stop after k iterations and print Res64 (default: full p-2 test)\n"
                "  -m      fused (default) or plain execution form\n"
                "  -H h    fused layout column length\n"
+               "  -I mode column passes: 1 in place, 2 in place + prefetch, -1 two buffers\n"
                "  -v -q   verbose / quiet\n");
 }
 
@@ -54,7 +56,7 @@ int fail(const char* what, int st) {
 
 int main(int argc, char** argv) {
   bool verbose = false, quiet = false;
-  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED;
+  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED, inplace = 0;
   long long freq = 0, k = 0;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
@@ -76,6 +78,7 @@ int main(int argc, char** argv) {
     else if (a == "-c") freq = std::atoll(next("-c"));
     else if (a == "-k") k = std::atoll(next("-k"));
     else if (a == "-H") fft_h = std::atoi(next("-H"));
+    else if (a == "-I") inplace = std::atoi(next("-I"));
     else if (a == "-m") {
       const std::string m = next("-m");
       if (m == "fused") mode = GL_MODE_FUSED;
@@ -116,6 +119,7 @@ int main(int argc, char** argv) {
   o.device = dev;
   o.mode = mode;
   o.fft_h = fft_h;
+  o.col_inplace = inplace;
   if (!N) {
     double ms = 0.0, err = 0.0;
     const int st = gl_find_signal_size(p, &o, &N, &ms, &err);
