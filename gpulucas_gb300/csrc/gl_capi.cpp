@@ -164,6 +164,7 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   g->ls_col = padded_stride(g->H);
   g->ls_row = padded_stride(g->W);
   g->sm_col = (size_t)2 * g->ls_col * 16;
+  g->sm_cinv = g->sm_col;
   g->sm_row = row_smem(g->W, g->pw);
   auto threads = [](int points, int per_thread, int cap) {
     int t = round_up32((points + per_thread - 1) / per_thread);
@@ -182,11 +183,11 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
       if (g->H / R > per * g->t_col) return GL_ERR_SIZE;
     }
     g->col_ip = 1;
-    g->sm_col = (size_t)g->ls_col * 16;
+    g->sm_col = g->sm_cinv = (size_t)g->ls_col * 16;
     if (pf) {
       if (g->H % 8) return GL_ERR_SIZE;  // bulk copies of 2H bytes must be 16-byte multiples
       g->col_pf = 1;
-      g->sm_col += (size_t)18 * g->H;
+      g->sm_cinv += (size_t)18 * g->H;
     }
   }
   return GL_OK;

@@ -55,7 +55,8 @@ struct FusedGeom {
                              // so more threads per line, for lengths too short to fill the GPU
   int ls_col, ls_row;        // padded shared-memory line strides (complex)
   int t_col, t_row;          // threads per CTA
-  size_t sm_col, sm_row;     // dynamic shared memory bytes
+  size_t sm_col, sm_row;     // dynamic shared memory bytes (sm_col: forward column pass)
+  size_t sm_cinv;            // inverse column pass (sm_col plus its prefetch area)
   LinePlan pw, ph;
 };
 

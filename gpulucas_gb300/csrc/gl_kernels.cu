@@ -585,7 +585,8 @@ static cudaError_t set_col_fwd_smem(int bytes) {
 // The attribute is per kernel and process-wide, shared by every plan: it is raised to the
 // layout chooser's bound once (a launch's occupancy follows its own dynamic size).
 cudaError_t set_fused_smem_limits(const FusedGeom& g) {
-  if (g.sm_col > (size_t)kMaxDynSmem || g.sm_row > (size_t)kMaxDynSmem) return cudaErrorInvalidValue;
+  if (g.sm_col > (size_t)kMaxDynSmem || g.sm_cinv > (size_t)kMaxDynSmem || g.sm_row > (size_t)kMaxDynSmem)
+    return cudaErrorInvalidValue;
   cudaError_t e;
   if ((e = set_col_fwd_smem<false, false>(kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<true, false>(kMaxDynSmem))) return e;
@@ -618,9 +619,9 @@ static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s
 }
 
 static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_col, s>>>(a);
-  else if (g.col_ip) k_col_inv<true, false><<<a.W, g.t_col, g.sm_col, s>>>(a);
-  else k_col_inv<false, false><<<a.W, g.t_col, g.sm_col, s>>>(a);
+  if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
+  else if (g.col_ip) k_col_inv<true, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
+  else k_col_inv<false, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
 }
 
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state) {
