@@ -122,8 +122,7 @@ def test_inplace_column_passes_match(gl, orc, p, N, H, mode):
     the two-buffer form, and the oracle's."""
     with gl.Plan(p, N, col_inplace=mode, fft_h=H, autotune=0) as a, \
             gl.Plan(p, N, col_inplace=-1, fft_h=H, autotune=0) as b:
-        extra = 18 * H if mode == 2 else 0
-        assert b.info.smem_col == 2 * (a.info.smem_col - extra)
+        assert b.info.smem_col == 2 * a.info.smem_col   # the forward column pass's buffer
         a.iterate(7)
         b.iterate(7)
         pa = a.products()
