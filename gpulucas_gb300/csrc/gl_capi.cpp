@@ -67,7 +67,6 @@ double line_ops(const LinePlan& lp) {
     switch (r) {
       case 3: return 14.0;
       case 5: return 36.0;
-      case 9: return 100.0;  // six DFT_3 and four internal twiddles
       default: return 72.0;  // 7
     }
   };

@@ -329,41 +329,6 @@ GL_HD void layered_dit(cplx* x, const cplx* tv) {
   for (int i = 0; i < R; ++i) x[i] = y[i];
 }
 
-#define GL_C91 0.7660444431189780352024   // cos(2pi/9)
-#define GL_S91 0.6427876096865393263226   // sin(2pi/9)
-#define GL_C92 0.1736481776669303488517   // cos(4pi/9)
-#define GL_S92 0.9848077530122080593667   // sin(4pi/9)
-#define GL_C94 -0.9396926207859083840541  // cos(8pi/9)
-#define GL_S94 0.3420201433256687330441   // sin(8pi/9)
-
-// DFT_9 as 3 x 3 (n = 3 n1 + n2, k = k1 + 3 k2): three DFT_3 over n1, the internal
-// twiddles w9^(n2 k1) (w9 = exp(S 2 pi i / 9)), three DFT_3 over n2.  One radix-9 stage
-// replaces two radix-3 stages at the same FP64 count with one barrier and one shared-memory
-// pass fewer.
-template <int S>
-GL_HD void dft9(cplx* x) {
-  cplx a[3][3];
-#pragma unroll
-  for (int n2 = 0; n2 < 3; ++n2) {
-    cplx t[3] = {x[n2], x[3 + n2], x[6 + n2]};
-    dft3<S>(t);
-#pragma unroll
-    for (int k1 = 0; k1 < 3; ++k1) a[n2][k1] = t[k1];
-  }
-  // w^1, w^2 on n2 = 1; w^2, w^4 on n2 = 2
-  a[1][1] = cmul(a[1][1], mk(GL_C91, S * GL_S91));
-  a[1][2] = cmul(a[1][2], mk(GL_C92, S * GL_S92));
-  a[2][1] = cmul(a[2][1], mk(GL_C92, S * GL_S92));
-  a[2][2] = cmul(a[2][2], mk(GL_C94, S * GL_S94));
-#pragma unroll
-  for (int k1 = 0; k1 < 3; ++k1) {
-    cplx t[3] = {a[0][k1], a[1][k1], a[2][k1]};
-    dft3<S>(t);
-#pragma unroll
-    for (int k2 = 0; k2 < 3; ++k2) x[k1 + 3 * k2] = t[k2];
-  }
-}
-
 template <int R, int S>
 GL_HD void dft(cplx* x) {
   if constexpr (R == 2) dft2<S>(x);
@@ -372,7 +337,6 @@ GL_HD void dft(cplx* x) {
   else if constexpr (R == 5) dft5<S>(x);
   else if constexpr (R == 7) dft7<S>(x);
   else if constexpr (R == 8) dft8<S>(x);
-  else if constexpr (R == 9) dft9<S>(x);
   else if constexpr (R == 16) dft16<S>(x);
 }
 

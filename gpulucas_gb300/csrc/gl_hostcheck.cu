@@ -16,7 +16,6 @@ static void run_dft(int R, cplx* x) {
     case 5: dft<5, S>(x); break;
     case 7: dft<7, S>(x); break;
     case 8: dft<8, S>(x); break;
-    case 9: dft<9, S>(x); break;
     case 16: dft<16, S>(x); break;
     default: break;
   }
@@ -26,7 +25,7 @@ extern "C" {
 
 // in-place DFT of R interleaved complex doubles; sign -1 forward, +1 inverse
 int hc_dft(int R, int sign, double* xy) {
-  if (R != 2 && R != 3 && R != 4 && R != 5 && R != 7 && R != 8 && R != 9 && R != 16) return -1;
+  if (R != 2 && R != 3 && R != 4 && R != 5 && R != 7 && R != 8 && R != 16) return -1;
   cplx* x = reinterpret_cast<cplx*>(xy);
   if (sign < 0) run_dft<-1>(R, x);
   else run_dft<1>(R, x);

@@ -144,10 +144,9 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
     const TW* st = tw + lp.off[s];
-    static_assert(kMaxRadix == 8, "line plans use radices 2, 4, 8, 3, 5, 7, 9");
+    static_assert(kMaxRadix == 8, "line plans use radices 2, 4, 8, 3, 5, 7");
     switch (lp.radix[s]) {
       case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, st); break;
-      case 9: stockham_stage<9, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 3: stockham_stage<3, S>(a, b, nlines, ls, lp.L, Ns, st); break;
@@ -236,7 +235,6 @@ __device__ __forceinline__ cplx* line_fft_ip(cplx* a, int nlines, int ls, const 
     const TW* st = tw + lp.off[s];
     switch (lp.radix[s]) {
       case 8: stockham_stage_ip<8, S>(a, nlines, ls, lp.L, Ns, st); break;
-      case 9: stockham_stage_ip<9, S>(a, nlines, ls, lp.L, Ns, st); break;
       case 4: stockham_stage_ip<4, S>(a, nlines, ls, lp.L, Ns, st); break;
       case 2: stockham_stage_ip<2, S>(a, nlines, ls, lp.L, Ns, st); break;
       case 3: stockham_stage_ip<3, S>(a, nlines, ls, lp.L, Ns, st); break;

@@ -263,12 +263,6 @@ std::vector<int> radix_plan(int n, int max_radix) {
       m /= q;
     }
   }
-  // pairs of 3 as one radix-9 stage (same FP64 count, one stage fewer) when the plan
-  // allows radix 8
-  while (max_radix >= 8 && m % 9 == 0) {
-    r.push_back(9);
-    m /= 9;
-  }
   const int odd[3] = {3, 5, 7};
   for (int q : odd) {
     while (m % q == 0) {

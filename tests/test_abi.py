@@ -64,7 +64,7 @@ def test_describe_layouts(gl, p, N, mode):
         rh = [r for r in info.radix_h if r]
         prod = lambda xs: eval("*".join(map(str, xs))) if xs else 1  # noqa: E731
         assert prod(rw) == info.fft_w and prod(rh) == info.fft_h
-        assert set(rw + rh) <= {2, 3, 4, 5, 7, 8, 9}
+        assert set(rw + rh) <= {2, 3, 4, 5, 7, 8}
         assert info.cols_per_cta == 1
         ls = lambda L: L + L // 16 + 1  # noqa: E731  padded line stride
         assert info.smem_col == 2 * ls(info.fft_h) * 16 <= 110 * 1024
