@@ -153,6 +153,7 @@ def _load():
         "gl_get_carry_state": (ctypes.c_int, [P, vp, vp]),
         "gl_set_products": (ctypes.c_int, [P, vp, ctypes.c_int64]),
         "gl_set_carry_state": (ctypes.c_int, [P, vp, vp, ctypes.c_int64]),
+        "gl_iterate_host": (ctypes.c_int, [P, vp, vp, ctypes.c_int64, vp, vp, ctypes.POINTER(IterReport)]),
         "gl_get_residue": (ctypes.c_int, [P, vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
         "errorTest": (ctypes.c_float, [ctypes.c_int, ctypes.c_int]),
         "mersenneTest": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
@@ -223,6 +224,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query", "gl_fast_signal_size",
     "gl_server_default_opts", "gl_server_create", "gl_server_submit", "gl_server_poll", "gl_server_drain",
     "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy", "gl_selftest_bounded_wait",
+    "gl_iterate_host",
 ]))
 
 
@@ -339,6 +341,18 @@ class Plan:
         h = np.empty(self.N, np.int8)
         _check(lib.gl_get_carry_state(self._h, _ptr(d), _ptr(h)), "carry_state")
         return d, h
+
+    def iterate_host(self, digit: np.ndarray, hi: np.ndarray, iters: int, check: bool = True):
+        """(digit, hi, report): `iters` iterations from a host-held carry-save state."""
+        d = np.ascontiguousarray(digit, np.int32)
+        h = np.ascontiguousarray(hi, np.int8)
+        do = np.empty(self.N, np.int32)
+        ho = np.empty(self.N, np.int8)
+        rep = IterReport()
+        st = lib.gl_iterate_host(self._h, _ptr(d), _ptr(h), int(iters), _ptr(do), _ptr(ho), ctypes.byref(rep))
+        if check:
+            _check(st, "iterate_host")
+        return do, ho, rep
 
     def set_carry_state(self, digit: np.ndarray, hi: np.ndarray, iterations: int):
         d = np.ascontiguousarray(digit, np.int32)

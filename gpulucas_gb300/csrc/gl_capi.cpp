@@ -914,6 +914,48 @@ static int ensure_carry(gl_plan* pl) {
   return GL_OK;
 }
 
+int gl_iterate_host(gl_plan* pl, const int32_t* digit_in, const int8_t* hi_in, int64_t iters, int32_t* digit_out,
+                    int8_t* hi_out, gl_iter_report* rep) {
+  if (!pl || !digit_in || !hi_in || !digit_out || !hi_out || iters < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  const size_t N = (size_t)pl->N;
+  GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->args.digit, digit_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->args.hi, hi_in, N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream));
+  pl->from_state = pl->mode == GL_MODE_FUSED;
+  pl->carry_valid = true;
+  if (iters > 0) {
+    const int rc = enqueue(pl, iters);
+    if (rc != GL_OK) return rc;
+    pl->iters_done += iters;
+    pl->carry_valid = pl->mode == GL_MODE_PLAIN;
+  }
+  const int rc = ensure_carry(pl);
+  if (rc != GL_OK) return rc;
+  GL_CUDA(cudaMemcpyAsync(digit_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(hi_out, pl->args.hi, N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
+  GL_CUDA(cudaEventSynchronize(pl->ev1));
+  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
+  if (e > pl->run_maxerr) pl->run_maxerr = e;
+  int st = GL_OK;
+  if (pl->h_status->flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
+  else if (pl->h_status->flags) st = GL_ERR_OVERFLOW;
+  else if (e >= pl->error_limit) st = GL_ERR_ROUNDOFF;
+  float ms = 0.f;
+  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
+  if (rep) {
+    rep->iterations = iters;
+    rep->total_iterations = pl->iters_done;
+    rep->max_roundoff = e;
+    rep->ms = ms;
+    rep->status = st;
+  }
+  return st;
+}
+
 int gl_get_carry_state(gl_plan* pl, int32_t* digit_out, int8_t* hi_out) {
   if (!pl || !digit_out || !hi_out) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));

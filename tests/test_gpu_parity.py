@@ -209,6 +209,22 @@ def test_roundoff_abort_is_reported(gl):
         assert rep.iterations < 2000
 
 
+@pytest.mark.parametrize("p,N,mode", [(44497, 2048, 0), (100003, 5184, 0), (1000003, 54432, 0), (100003, 5184, 1)])
+def test_iterate_host_state_chain(gl, orc, p, N, mode):
+    """gl_iterate_host from a host-held carry-save state, step after step, follows the
+    oracle's iteration exactly (both forms; N = 2048 runs the resident form)."""
+    o = orc.IBDWT(p, N)
+    d, h = o.state()
+    with gl.Plan(p, N, mode=mode) as pl:
+        for k in (1, 3, 1, 10):
+            d, h, rep = pl.iterate_host(d, h, k)
+            o.iterate(k)
+            d2, h2 = o.state()
+            assert rep.status == 0 and (d == d2).all() and (h == h2).all()
+        pl.set_carry_state(d, h, 15)
+        assert pl.res64() == orc.Exact(p).iterate(15).res64()
+
+
 def test_bounded_wait_times_out_and_device_stays_usable(gl, orc):
     """A kernel waiting on a barrier that nothing completes gives up after its bound,
     the host reads GL_ERR_TIMEOUT, and the context keeps working (no trap, no hang)."""
