@@ -50,10 +50,10 @@ bool fill_line_plan(int L, LinePlan* lp, int max_radix = kMaxRadix) {
 
 int round_up32(int x) { return (x + 31) / 32 * 32; }
 
-// FP64 instructions per point of one line DFT with the given radices: power-of-two
-// stages run the layered FMA-merged DIT (first stage: constant twiddles only, later
-// stages: 3 instructions per point and bit); odd radices run DFT_R plus one complex
-// twiddle product per non-first-stage input.
+// FP64 instructions per point of one line DFT with the given radices.  First stage:
+// constant twiddles only (layered DIT, DFT_R).  Later stages: radices 8, 4, 3 in ratio
+// form (66, 22, 16 instructions per butterfly), 2 and 16 the layered DIT (3 per point and
+// bit), 5 and 7 DFT_R plus one complex product per input.
 double line_ops(const LinePlan& lp) {
   auto first_pow2 = [](int r) {
     switch (r) {
@@ -76,7 +76,8 @@ double line_ops(const LinePlan& lp) {
     const bool pow2 = (r & (r - 1)) == 0;
     int lg = 0;
     while ((1 << lg) < r) ++lg;
-    if (pow2) ops += s ? 3.0 * lg : first_pow2(r);
+    if (s && (r == 8 || r == 4 || r == 3)) ops += (r == 8 ? 66.0 : r == 4 ? 22.0 : 16.0) / r;
+    else if (pow2) ops += s ? 3.0 * lg : first_pow2(r);
     else ops += odd_ops(r) / r + (s ? 4.0 * (r - 1) / r : 0.0);
   }
   return ops;

@@ -341,6 +341,166 @@ GL_HD void dft(cplx* x) {
 }
 
 // ---------------------------------------------------------------------------
+// Twiddled radix-8, -4 and -3 stages in ratio form, after S. Goedecker, "Fast radix 2,
+// 3, 4, and 5 kernels for fast Fourier transformations on computers with overlapping
+// multiply-add instructions", SIAM J. Sci. Comput. 18 (1997) 1605-1611.  Each external
+// twiddle w^q (forward direction) is stored as
+//     w^q = i^f rho_q (1 + i tau_q),   |tau_q| <= 1, f in {0, 1}, |rho_q| >= 1/sqrt2:
+// the input is rotated by i^f (register moves and a sign bit, no FP64 instruction),
+// multiplied by (1 + i tau_q) (2 FMA), and the real factors rho_q ride in the FMAs of
+// the DFT that follows as ratios of the two inputs each sum combines (sigma = rho_a /
+// rho_b), so every sum or difference costs 2 FMA.  FP64 instructions per butterfly:
+// radix 8: 66 (layered DIT with complex twiddles: 72), radix 4: 22 (24), radix 3: 16
+// (two complex products and DFT_3: 22).  The inverse direction (S = +1) uses the same
+// stored values for conj(w^q): rotation by -i, tau -> -tau.
+//
+// Stored doubles per butterfly position (pairs of them per 16-byte slot):
+//   R = 8: tau1..tau7, flags, rho4, rho6/rho2, rho2, rho5/rho1, rho7/rho3, rho3/rho1,
+//          rho1, rho1/sqrt2
+//   R = 4: tau1, tau2, tau3, flags, rho2, rho3/rho1, rho1, 0
+//   R = 3: tau1, tau2, rho2/rho1, flags, rho1, rho1/2, rho1 sin(2pi/3), 0
+// flags: bit q = f of w^q, held as the bit pattern of the double.
+// ---------------------------------------------------------------------------
+template <int R>
+GL_HD constexpr bool ratio_stage() {
+  return R == 3 || R == 4 || R == 8;
+}
+
+// (1 + i tau) i^f x for S = -1; (1 - i tau) (-i)^f x for S = +1
+template <int S>
+GL_HD cplx prerot(cplx x, double tau, unsigned f) {
+  constexpr unsigned long long kNeg = 0x8000000000000000ull;
+  const unsigned long long re = (unsigned long long)dbl_bits(x.re), im = (unsigned long long)dbl_bits(x.im);
+  // rotation by -S i: forward (re, im) -> (-im, re), inverse (re, im) -> (im, -re)
+  const unsigned long long xr = f ? (im ^ (S < 0 ? kNeg : 0ull)) : re;
+  const unsigned long long xi = f ? (re ^ (S < 0 ? 0ull : kNeg)) : im;
+  const double a = bits_dbl((long long)xr), b = bits_dbl((long long)xi);
+  return mk(fma(S < 0 ? -tau : tau, b, a), fma(S < 0 ? tau : -tau, a, b));
+}
+// a + l b, l real: 2 FMA
+GL_HD cplx axpy(double l, cplx b, cplx a) { return mk(fma(l, b.re, a.re), fma(l, b.im, a.im)); }
+// a + S i l b, l real: 2 FMA
+template <int S>
+GL_HD cplx axpy_si(double l, cplx b, cplx a) {
+  return mk(fma(S < 0 ? l : -l, b.im, a.re), fma(S < 0 ? -l : l, b.re, a.im));
+}
+GL_HD unsigned flag_bits(double v) { return (unsigned)dbl_bits(v); }
+
+// slot(i) returns the i-th 16-byte slot of this butterfly's stored values; the values
+// are read where they are used, so few of them are live at once.
+template <int S, typename Slot>
+GL_HD void ratio_r8(cplx* v, const Slot& slot) {
+  const cplx s3 = slot(3);
+  const unsigned fl = flag_bits(s3.im);
+  cplx u[8];
+  u[0] = v[0];
+  {
+    const cplx s0 = slot(0), s1 = slot(1), s2 = slot(2);
+    u[1] = prerot<S>(v[1], s0.re, (fl >> 1) & 1);
+    u[2] = prerot<S>(v[2], s0.im, (fl >> 2) & 1);
+    u[3] = prerot<S>(v[3], s1.re, (fl >> 3) & 1);
+    u[4] = prerot<S>(v[4], s1.im, (fl >> 4) & 1);
+    u[5] = prerot<S>(v[5], s2.re, (fl >> 5) & 1);
+    u[6] = prerot<S>(v[6], s2.im, (fl >> 6) & 1);
+    u[7] = prerot<S>(v[7], s3.re, (fl >> 7) & 1);
+  }
+  const cplx s4 = slot(4), s5 = slot(5), s6 = slot(6), s7 = slot(7);
+  // even inputs: DFT_4 of (u0, rho2 u2, rho4 u4, rho6 u6)
+  const cplx a0 = axpy(s4.re, u[4], u[0]), a1 = axpy(-s4.re, u[4], u[0]);
+  const cplx b0 = axpy(s4.im, u[6], u[2]), b1 = axpy(-s4.im, u[6], u[2]);
+  const cplx e0 = axpy(s5.re, b0, a0), e2 = axpy(-s5.re, b0, a0);
+  const cplx e1 = axpy_si<S>(s5.re, b1, a1), e3 = axpy_si<S>(-s5.re, b1, a1);
+  // odd inputs over rho1: DFT_4 of (u1, (rho3/rho1) u3, (rho5/rho1) u5, (rho7/rho1) u7)
+  const cplx c0 = axpy(s5.im, u[5], u[1]), c1 = axpy(-s5.im, u[5], u[1]);
+  const cplx d0 = axpy(s6.re, u[7], u[3]), d1 = axpy(-s6.re, u[7], u[3]);
+  const cplx o0 = axpy(s6.im, d0, c0), o2 = axpy(-s6.im, d0, c0);
+  const cplx o1 = axpy_si<S>(s6.im, d1, c1), o3 = axpy_si<S>(-s6.im, d1, c1);
+  // y_p = E_p + W8^p rho1 O_p, y_(p+4) = E_p - W8^p rho1 O_p
+  v[0] = axpy(s7.re, o0, e0);
+  v[4] = axpy(-s7.re, o0, e0);
+  v[2] = axpy_si<S>(s7.re, o2, e2);
+  v[6] = axpy_si<S>(-s7.re, o2, e2);
+  // W8 = (1 + S i)/sqrt2, W8^3 = (-1 + S i)/sqrt2; s7.im = rho1/sqrt2
+  const cplx t1 = S < 0 ? mk(o1.re + o1.im, o1.im - o1.re) : mk(o1.re - o1.im, o1.im + o1.re);
+  const cplx t3 = S < 0 ? mk(o3.im - o3.re, -o3.im - o3.re) : mk(-o3.re - o3.im, o3.re - o3.im);
+  v[1] = axpy(s7.im, t1, e1);
+  v[5] = axpy(-s7.im, t1, e1);
+  v[3] = axpy(s7.im, t3, e3);
+  v[7] = axpy(-s7.im, t3, e3);
+}
+
+template <int S, typename Slot>
+GL_HD void ratio_r4(cplx* v, const Slot& slot) {
+  const cplx s0 = slot(0), s1 = slot(1);
+  const unsigned fl = flag_bits(s1.im);
+  const cplx u1 = prerot<S>(v[1], s0.re, (fl >> 1) & 1);
+  const cplx u2 = prerot<S>(v[2], s0.im, (fl >> 2) & 1);
+  const cplx u3 = prerot<S>(v[3], s1.re, (fl >> 3) & 1);
+  const cplx s2 = slot(2), s3 = slot(3);
+  const cplx a0 = axpy(s2.re, u2, v[0]), a1 = axpy(-s2.re, u2, v[0]);
+  const cplx b0 = axpy(s2.im, u3, u1), b1 = axpy(-s2.im, u3, u1);
+  v[0] = axpy(s3.re, b0, a0);
+  v[2] = axpy(-s3.re, b0, a0);
+  v[1] = axpy_si<S>(s3.re, b1, a1);
+  v[3] = axpy_si<S>(-s3.re, b1, a1);
+}
+
+template <int S, typename Slot>
+GL_HD void ratio_r3(cplx* v, const Slot& slot) {
+  const cplx s0 = slot(0), s1 = slot(1);
+  const unsigned fl = flag_bits(s1.im);
+  const cplx u1 = prerot<S>(v[1], s0.re, (fl >> 1) & 1);
+  const cplx u2 = prerot<S>(v[2], s0.im, (fl >> 2) & 1);
+  const cplx s2 = slot(2), s3 = slot(3);
+  const cplx t = axpy(s1.re, u2, u1), d = axpy(-s1.re, u2, u1);
+  const cplx m = axpy(-s2.im, t, v[0]);
+  v[0] = axpy(s2.re, t, v[0]);
+  v[1] = axpy_si<S>(s3.re, d, m);
+  v[2] = axpy_si<S>(-s3.re, d, m);
+}
+
+// Stored 16-byte slots per butterfly position of a twiddled stage of radix R.
+template <int R>
+GL_HD constexpr int stage_slots() {
+  return R == 8 ? 8 : (R == 4 || R == 3) ? 4 : ((R & (R - 1)) == 0 ? (R == 2 ? 1 : R / 2) : R - 1);
+}
+
+// One butterfly of a Stockham stage: DFT_R of v[q] w^q (w^q = 1 in the first stage,
+// Ns == 1).  slot(i) reads the stage's i-th stored slot of this butterfly position.
+// Radices 8, 4, 3 use the ratio form; 2 and 16 the layered DIT with complex values
+// (level values w^(R/2^l) W_(2^l)^p, conjugated here for S = +1); 5 and 7 a complex
+// product per input and DFT_R.
+template <int R, int S, typename Slot>
+GL_HD void stage_dft(cplx* v, bool twiddled, const Slot& slot) {
+  constexpr bool POW2 = (R & (R - 1)) == 0;
+  if (!twiddled) {
+    if constexpr (POW2) layered_dit<R, S, false>(v, nullptr);
+    else dft<R, S>(v);
+  } else if constexpr (R == 8) {
+    ratio_r8<S>(v, slot);
+  } else if constexpr (R == 4) {
+    ratio_r4<S>(v, slot);
+  } else if constexpr (R == 3) {
+    ratio_r3<S>(v, slot);
+  } else {
+    constexpr int NV = stage_slots<R>();
+    cplx tv[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      const cplx t = slot(i);
+      tv[i] = S < 0 ? t : conj(t);
+    }
+    if constexpr (POW2) {
+      layered_dit<R, S, true>(v, tv);
+    } else {
+#pragma unroll
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tv[q - 1]);
+      dft<R, S>(v);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // integer-domain conversions
 // ---------------------------------------------------------------------------
 

@@ -145,3 +145,63 @@ void hc_pair_coeff(int k, int M, double* c) {
 }
 
 }  // extern "C"
+
+// One line DFT of length L with the given radices, run on the host through the device
+// butterfly (stage_dft) and the product's stage-ordered table, in the Stockham order of
+// the kernels' shared-memory stages (without the padding).  sign -1 forward, +1 inverse
+// (unscaled).  Returns 0, or -1 for an unsupported radix.
+namespace {
+struct TableSlot {
+  const cplx* tw;
+  int Ns, k;
+  __host__ __device__ cplx operator()(int i) const { return tw[(size_t)i * Ns + k]; }
+};
+
+template <int S>
+int host_stage(int R, const cplx* src, cplx* dst, int L, int Ns, const cplx* tw) {
+  const int LR = L / R;
+  for (int j = 0; j < LR; ++j) {
+    const int k = j % Ns;
+    cplx v[16];
+    for (int q = 0; q < R; ++q) v[q] = src[j + q * LR];
+    const TableSlot slot{tw, Ns, k};
+    const bool t = Ns > 1;
+    switch (R) {
+      case 2: stage_dft<2, S>(v, t, slot); break;
+      case 3: stage_dft<3, S>(v, t, slot); break;
+      case 4: stage_dft<4, S>(v, t, slot); break;
+      case 5: stage_dft<5, S>(v, t, slot); break;
+      case 7: stage_dft<7, S>(v, t, slot); break;
+      case 8: stage_dft<8, S>(v, t, slot); break;
+      case 16: stage_dft<16, S>(v, t, slot); break;
+      default: return -1;
+    }
+    const int base = (j - k) * R + k;
+    for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+  }
+  return 0;
+}
+}  // namespace
+
+extern "C" int hc_line_fft(int L, const int* radices, int nst, int sign, double* xy) {
+  std::vector<int> r(radices, radices + nst);
+  std::vector<gl::HostCplx> tw;
+  int off[16];
+  if (nst > 16) return -1;
+  gl::stage_twiddles(L, r, tw, off);
+  std::vector<cplx> a(reinterpret_cast<cplx*>(xy), reinterpret_cast<cplx*>(xy) + L), b((size_t)L);
+  const cplx* t = reinterpret_cast<const cplx*>(tw.data());
+  int Ns = 1;
+  for (int s = 0; s < nst; ++s) {
+    const int st = sign < 0 ? host_stage<-1>(r[s], a.data(), b.data(), L, Ns, t + off[s])
+                            : host_stage<1>(r[s], a.data(), b.data(), L, Ns, t + off[s]);
+    if (st) return st;
+    Ns *= r[s];
+    a.swap(b);
+  }
+  for (int i = 0; i < L; ++i) {
+    xy[2 * i] = a[i].re;
+    xy[2 * i + 1] = a[i].im;
+  }
+  return 0;
+}

@@ -92,14 +92,12 @@ __device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
 // Stockham DIT stage, out of place (src -> dst, one barrier).  Butterfly j of a
 // line reads x[j + q L/R], applies the external twiddle w^q with
 // w = w_L^((j mod Ns) L/(Ns R)), does DFT_R and writes x[(j - j mod Ns) R + j mod Ns +
-// p Ns].  Power-of-two radices run the layered FMA-merged DIT (its per-level twiddle
-// values come from the stage-ordered table at off + v Ns + k); odd radices multiply
-// by w^q from the table and run DFT_R.
+// p Ns].  The butterfly itself is stage_dft (gl_device.cuh); its stored values for
+// position k are the slots off + v Ns + k of the stage-ordered table, so lanes with
+// consecutive k read consecutive slots.
 template <int R, int S, typename TW>
 __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cplx* __restrict__ dst, int nlines,
                                                int ls, int L, int Ns, const TW* __restrict__ tw) {
-  constexpr bool POW2 = (R & (R - 1)) == 0;
-  constexpr int NV = POW2 ? (R == 2 ? 1 : R / 2) : R - 1;
   const int LR = L / R;
   const int nb = nlines * LR;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -110,24 +108,8 @@ __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cpl
     cplx v[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = s[pad(j + q * LR)];
-    if (Ns > 1) {
-      cplx tv[NV];
-#pragma unroll
-      for (int i = 0; i < NV; ++i) {
-        const cplx t = tw_at(tw + (size_t)i * Ns + k);
-        tv[i] = S < 0 ? t : conj(t);
-      }
-      if constexpr (POW2) {
-        layered_dit<R, S, true>(v, tv);
-      } else {
-#pragma unroll
-        for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tv[q - 1]);
-        dft<R, S>(v);
-      }
-    } else {
-      if constexpr (POW2) layered_dit<R, S, false>(v, nullptr);
-      else dft<R, S>(v);
-    }
+    const TW* tk = tw + k;
+    stage_dft<R, S>(v, Ns > 1, [&](int i) { return tw_at(tk + (size_t)i * Ns); });
     cplx* d = dst + l * ls;
     const int base = (j - k) * R + k;
 #pragma unroll
@@ -174,8 +156,6 @@ __host__ __device__ constexpr int ip_butterflies() {
 template <int R, int S, typename TW>
 __device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nlines, int ls, int L, int Ns,
                                                   const TW* __restrict__ tw) {
-  constexpr bool POW2 = (R & (R - 1)) == 0;
-  constexpr int NV = POW2 ? (R == 2 ? 1 : R / 2) : R - 1;
   constexpr int B = ip_butterflies<R>();
   const int LR = L / R;
   const int nb = nlines * LR;
@@ -201,24 +181,8 @@ __device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nl
       cplx v[R];
 #pragma unroll
       for (int q = 0; q < R; ++q) v[q] = held[i * R + q];
-      if (Ns > 1) {
-        cplx tv[NV];
-#pragma unroll
-        for (int t = 0; t < NV; ++t) {
-          const cplx w = tw_at(tw + (size_t)t * Ns + k);
-          tv[t] = S < 0 ? w : conj(w);
-        }
-        if constexpr (POW2) {
-          layered_dit<R, S, true>(v, tv);
-        } else {
-#pragma unroll
-          for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tv[q - 1]);
-          dft<R, S>(v);
-        }
-      } else {
-        if constexpr (POW2) layered_dit<R, S, false>(v, nullptr);
-        else dft<R, S>(v);
-      }
+      const TW* tk = tw + k;
+      stage_dft<R, S>(v, Ns > 1, [&](int t) { return tw_at(tk + (size_t)t * Ns); });
       cplx* d = buf + l * ls;
       const int base = (j - k) * R + k;
 #pragma unroll

@@ -9,6 +9,7 @@
 #include "gl_tables.h"
 
 #include <cmath>
+#include <cstring>
 #include <thread>
 #include <vector>
 
@@ -210,12 +211,75 @@ void twiddle_table(int64_t L, std::vector<HostCplx>& tw) {
 int stage_values(int R) {
   switch (R) {
     case 2: return 1;
-    case 4: return 2;
-    case 8: return 4;
+    case 3: return 4;
+    case 4: return 4;
+    case 8: return 8;
     case 16: return 8;
     default: return R - 1;
   }
 }
+
+namespace {
+// w_L^t = cos(2 pi t/L) - i sin(2 pi t/L) = i^f rho (1 + i tau) with |tau| <= 1: f = 1 in
+// the octants where |sin| >= |cos| (decided on the integer angle, so it is exact).
+struct RatioForm {
+  DD rho, tau;
+  int f;
+};
+RatioForm ratio_form(int64_t t, int64_t L) {
+  t %= L;
+  if (t < 0) t += L;
+  DD C, S;
+  cos_sin_dd(t, L, &C, &S);
+  const DD re = C, im = -S;
+  const int64_t o = (8 * t) / L;
+  RatioForm r;
+  if (o == 1 || o == 2 || o == 5 || o == 6) {
+    r.f = 1;  // i rho (1 + i tau) = -rho tau + i rho
+    r.rho = im;
+    r.tau = -(re / im);
+  } else {
+    r.f = 0;
+    r.rho = re;
+    r.tau = im / re;
+  }
+  return r;
+}
+
+// The stored doubles of one position of a twiddled radix-8, -4 or -3 stage (the ratio
+// form the device butterflies read): w = w_L^e.
+void ratio_values(int R, int64_t e, int64_t L, double* out) {
+  RatioForm w[8];
+  uint64_t fl = 0;
+  for (int q = 1; q < R; ++q) {
+    w[q] = ratio_form(e * q, L);
+    fl |= (uint64_t)w[q].f << q;
+  }
+  double flags;
+  std::memcpy(&flags, &fl, sizeof flags);
+  auto rd = [](DD x) { return to_double(x); };
+  auto ratio = [&](int a, int b) { return to_double(w[a].rho / w[b].rho); };
+  if (R == 8) {
+    DD c45, s45;
+    sincos_octant(1, 1, &s45, &c45);  // cos(pi/4)
+    const double v[16] = {rd(w[1].tau), rd(w[2].tau), rd(w[3].tau), rd(w[4].tau), rd(w[5].tau),
+                          rd(w[6].tau), rd(w[7].tau), flags,       rd(w[4].rho), ratio(6, 2),
+                          rd(w[2].rho), ratio(5, 1),  ratio(7, 3), ratio(3, 1),  rd(w[1].rho),
+                          rd(w[1].rho * c45)};
+    std::memcpy(out, v, sizeof v);
+  } else if (R == 4) {
+    const double v[8] = {rd(w[1].tau), rd(w[2].tau), rd(w[3].tau), flags, rd(w[2].rho), ratio(3, 1),
+                         rd(w[1].rho), 0.0};
+    std::memcpy(out, v, sizeof v);
+  } else {
+    DD c3, s3;
+    cos_sin_dd(1, 3, &c3, &s3);  // sin(2 pi/3)
+    const double v[8] = {rd(w[1].tau), rd(w[2].tau), ratio(2, 1), flags, rd(w[1].rho), 0.5 * rd(w[1].rho),
+                         rd(w[1].rho * s3), 0.0};
+    std::memcpy(out, v, sizeof v);
+  }
+}
+}  // namespace
 
 void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw, int* off) {
   std::vector<HostCplx> base;
@@ -232,7 +296,11 @@ void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx
       tw.resize(start + (size_t)nv * Ns);
       for (int k = 0; k < Ns; ++k) {
         const int64_t e = (int64_t)k * tws;  // exponent of w = w_L^e
-        if (R & (R - 1)) {
+        if (R == 8 || R == 4 || R == 3) {
+          double vals[16];
+          ratio_values(R, e, L, vals);
+          for (int v = 0; v < nv; ++v) tw[start + (size_t)v * Ns + k] = HostCplx{vals[2 * v], vals[2 * v + 1]};
+        } else if (R & (R - 1)) {
           for (int q = 1; q < R; ++q) tw[start + (size_t)(q - 1) * Ns + k] = base[(e * q) % L];
         } else {
           int v = 0;

@@ -130,3 +130,25 @@ def test_layered_dit(hc, R, sign, with_tw):
         xt = x * ww ** np.arange(R)
         ref = np.fft.fft(xt) if sign < 0 else np.fft.ifft(xt) * R
         assert np.abs(y - ref).max() <= 1e-14 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("radices", [[8, 8, 3, 3], [8, 8, 8, 4], [4, 3], [8, 4, 2], [3, 3, 3], [4, 4, 4, 4],
+                                     [8, 8, 8, 8, 3], [16, 8, 3], [8, 5, 7], [5, 4, 3], [2, 2, 2]])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_line_dft_through_stage_tables(hc, radices, sign):
+    """A whole line DFT through the device butterfly (stage_dft) and the product's
+    stage-ordered table, in the kernels' Stockham order: twiddled radix-8/4/3 stages in
+    ratio form, the others with complex values."""
+    f = hc.hc_line_fft
+    f.argtypes = [ctypes.c_int, np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"), ctypes.c_int,
+                  ctypes.c_int, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+    f.restype = ctypes.c_int
+    L = int(np.prod(radices))
+    rng = np.random.default_rng(L * 3 + sign)
+    x = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+    buf = np.empty(2 * L)
+    buf[0::2], buf[1::2] = x.real, x.imag
+    assert f(L, np.array(radices, np.int32), len(radices), sign, buf) == 0
+    y = buf[0::2] + 1j * buf[1::2]
+    ref = np.fft.fft(x) if sign < 0 else np.fft.ifft(x) * L
+    assert np.abs(y - ref).max() <= 2e-15 * np.abs(ref).max()
