@@ -346,7 +346,7 @@ GL_HD void dft(cplx* x) {
 // multiply-add instructions", SIAM J. Sci. Comput. 18 (1997) 1605-1611.  Each external
 // twiddle w^q (forward direction) is stored as
 //     w^q = i^f rho_q (1 + i tau_q),   |tau_q| <= 1, f in {0, 1}, |rho_q| >= 1/sqrt2:
-// the input is rotated by i^f (register moves and a sign bit, no FP64 instruction),
+// the input is rotated by i^f (register selects and a sign bit, no FP64 instruction),
 // multiplied by (1 + i tau_q) (2 FMA), and the real factors rho_q ride in the FMAs of
 // the DFT that follows as ratios of the two inputs each sum combines (sigma = rho_a /
 // rho_b), so every sum or difference costs 2 FMA.  FP64 instructions per butterfly:
@@ -354,9 +354,10 @@ GL_HD void dft(cplx* x) {
 // (two complex products and DFT_3: 22).  The inverse direction (S = +1) uses the same
 // stored values for conj(w^q): rotation by -i, tau -> -tau.
 //
-// Stored doubles per butterfly position (pairs of them per 16-byte slot):
-//   R = 8: tau1..tau7, flags, rho4, rho6/rho2, rho2, rho5/rho1, rho7/rho3, rho3/rho1,
-//          rho1, rho1/sqrt2
+// Stored doubles per butterfly position (pairs of them per 16-byte slot), tau_q stored
+// with the sign of f folded in (-tau_q where f = 1):
+//   R = 8: tau2, tau4, tau6, flags, rho4, rho6/rho2, rho2, rho5/rho1, tau1, tau5, tau3,
+//          tau7, rho7/rho3, rho3/rho1, rho1, rho1/sqrt2
 //   R = 4: tau1, tau2, tau3, flags, rho2, rho3/rho1, rho1, 0
 //   R = 3: tau1, tau2, rho2/rho1, flags, rho1, rho1/2, rho1 sin(2pi/3), 0
 // flags: bit q = f of w^q, held as the bit pattern of the double.
@@ -366,16 +367,29 @@ GL_HD constexpr bool ratio_stage() {
   return R == 3 || R == 4 || R == 8;
 }
 
-// (1 + i tau) i^f x for S = -1; (1 - i tau) (-i)^f x for S = +1
+// Sign of x flipped when f == 1, by an integer instruction on the high word.  Inline PTX
+// keeps the compiler from turning a sign-bit XOR back into an FP64 negation, which it
+// would issue as a DADD when the negated value feeds a select.
+GL_HD double flip_sign_if(double x, unsigned f) {
+#ifdef __CUDA_ARCH__
+  int hi = __double2hiint(x);
+  const int lo = __double2loint(x);
+  asm("xor.b32 %0, %0, %1;" : "+r"(hi) : "r"(f << 31));
+  return __hiloint2double(hi, lo);
+#else
+  return bits_dbl(dbl_bits(x) ^ (long long)((unsigned long long)f << 63));
+#endif
+}
+
+// Forward (S = -1): (1 + i tau) i^f x; inverse (S = +1): (1 - i tau) (-i)^f x.  The table
+// holds t = tau for f = 0 and t = -tau for f = 1; with (a, b) = (re, im) or (im, re):
+//   forward  u = (+-(a - t b), b + t a),   inverse  u = (a + t b, +-(b - t a)),
+// the sign flipped for f = 1.  2 FMA and integer instructions (selects, one XOR).
 template <int S>
-GL_HD cplx prerot(cplx x, double tau, unsigned f) {
-  constexpr unsigned long long kNeg = 0x8000000000000000ull;
-  const unsigned long long re = (unsigned long long)dbl_bits(x.re), im = (unsigned long long)dbl_bits(x.im);
-  // rotation by -S i: forward (re, im) -> (-im, re), inverse (re, im) -> (im, -re)
-  const unsigned long long xr = f ? (im ^ (S < 0 ? kNeg : 0ull)) : re;
-  const unsigned long long xi = f ? (re ^ (S < 0 ? 0ull : kNeg)) : im;
-  const double a = bits_dbl((long long)xr), b = bits_dbl((long long)xi);
-  return mk(fma(S < 0 ? -tau : tau, b, a), fma(S < 0 ? tau : -tau, a, b));
+GL_HD cplx prerot(cplx x, double t, unsigned f) {
+  const double a = f ? x.im : x.re, b = f ? x.re : x.im;
+  if (S < 0) return mk(flip_sign_if(fma(-t, b, a), f), fma(t, a, b));
+  return mk(fma(t, b, a), flip_sign_if(fma(-t, a, b), f));
 }
 // a + l b, l real: 2 FMA
 GL_HD cplx axpy(double l, cplx b, cplx a) { return mk(fma(l, b.re, a.re), fma(l, b.im, a.im)); }
@@ -387,35 +401,46 @@ GL_HD cplx axpy_si(double l, cplx b, cplx a) {
 GL_HD unsigned flag_bits(double v) { return (unsigned)dbl_bits(v); }
 
 // slot(i) returns the i-th 16-byte slot of this butterfly's stored values; the values
-// are read where they are used, so few of them are live at once.
+// are read where they are used, so few of them are live at once.  Radix 8 runs the even
+// inputs' DFT_4, then the odd inputs', then the combining level, so at most the even
+// results and the odd inputs are live between the halves.
 template <int S, typename Slot>
 GL_HD void ratio_r8(cplx* v, const Slot& slot) {
-  const cplx s3 = slot(3);
-  const unsigned fl = flag_bits(s3.im);
-  cplx u[8];
-  u[0] = v[0];
+  const cplx s1 = slot(1);
+  const unsigned fl = flag_bits(s1.im);
+  // even inputs: DFT_4 of (v0, rho2 u2, rho4 u4, rho6 u6)
+  cplx e0, e1, e2, e3;
+  double sig5;
   {
-    const cplx s0 = slot(0), s1 = slot(1), s2 = slot(2);
-    u[1] = prerot<S>(v[1], s0.re, (fl >> 1) & 1);
-    u[2] = prerot<S>(v[2], s0.im, (fl >> 2) & 1);
-    u[3] = prerot<S>(v[3], s1.re, (fl >> 3) & 1);
-    u[4] = prerot<S>(v[4], s1.im, (fl >> 4) & 1);
-    u[5] = prerot<S>(v[5], s2.re, (fl >> 5) & 1);
-    u[6] = prerot<S>(v[6], s2.im, (fl >> 6) & 1);
-    u[7] = prerot<S>(v[7], s3.re, (fl >> 7) & 1);
+    const cplx s0 = slot(0), s2 = slot(2), s3 = slot(3);
+    sig5 = s3.im;
+    const cplx u4 = prerot<S>(v[4], s0.im, (fl >> 4) & 1);
+    const cplx a0 = axpy(s2.re, u4, v[0]), a1 = axpy(-s2.re, u4, v[0]);
+    const cplx u2 = prerot<S>(v[2], s0.re, (fl >> 2) & 1);
+    const cplx u6 = prerot<S>(v[6], s1.re, (fl >> 6) & 1);
+    const cplx b0 = axpy(s2.im, u6, u2), b1 = axpy(-s2.im, u6, u2);
+    e0 = axpy(s3.re, b0, a0);
+    e2 = axpy(-s3.re, b0, a0);
+    e1 = axpy_si<S>(s3.re, b1, a1);
+    e3 = axpy_si<S>(-s3.re, b1, a1);
   }
-  const cplx s4 = slot(4), s5 = slot(5), s6 = slot(6), s7 = slot(7);
-  // even inputs: DFT_4 of (u0, rho2 u2, rho4 u4, rho6 u6)
-  const cplx a0 = axpy(s4.re, u[4], u[0]), a1 = axpy(-s4.re, u[4], u[0]);
-  const cplx b0 = axpy(s4.im, u[6], u[2]), b1 = axpy(-s4.im, u[6], u[2]);
-  const cplx e0 = axpy(s5.re, b0, a0), e2 = axpy(-s5.re, b0, a0);
-  const cplx e1 = axpy_si<S>(s5.re, b1, a1), e3 = axpy_si<S>(-s5.re, b1, a1);
   // odd inputs over rho1: DFT_4 of (u1, (rho3/rho1) u3, (rho5/rho1) u5, (rho7/rho1) u7)
-  const cplx c0 = axpy(s5.im, u[5], u[1]), c1 = axpy(-s5.im, u[5], u[1]);
-  const cplx d0 = axpy(s6.re, u[7], u[3]), d1 = axpy(-s6.re, u[7], u[3]);
-  const cplx o0 = axpy(s6.im, d0, c0), o2 = axpy(-s6.im, d0, c0);
-  const cplx o1 = axpy_si<S>(s6.im, d1, c1), o3 = axpy_si<S>(-s6.im, d1, c1);
+  cplx o0, o1, o2, o3;
+  {
+    const cplx s4 = slot(4), s5 = slot(5), s6 = slot(6);
+    const cplx u1 = prerot<S>(v[1], s4.re, (fl >> 1) & 1);
+    const cplx u5 = prerot<S>(v[5], s4.im, (fl >> 5) & 1);
+    const cplx c0 = axpy(sig5, u5, u1), c1 = axpy(-sig5, u5, u1);
+    const cplx u3 = prerot<S>(v[3], s5.re, (fl >> 3) & 1);
+    const cplx u7 = prerot<S>(v[7], s5.im, (fl >> 7) & 1);
+    const cplx d0 = axpy(s6.re, u7, u3), d1 = axpy(-s6.re, u7, u3);
+    o0 = axpy(s6.im, d0, c0);
+    o2 = axpy(-s6.im, d0, c0);
+    o1 = axpy_si<S>(s6.im, d1, c1);
+    o3 = axpy_si<S>(-s6.im, d1, c1);
+  }
   // y_p = E_p + W8^p rho1 O_p, y_(p+4) = E_p - W8^p rho1 O_p
+  const cplx s7 = slot(7);
   v[0] = axpy(s7.re, o0, e0);
   v[4] = axpy(-s7.re, o0, e0);
   v[2] = axpy_si<S>(s7.re, o2, e2);

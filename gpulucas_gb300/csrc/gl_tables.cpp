@@ -221,7 +221,8 @@ int stage_values(int R) {
 
 namespace {
 // w_L^t = cos(2 pi t/L) - i sin(2 pi t/L) = i^f rho (1 + i tau) with |tau| <= 1: f = 1 in
-// the octants where |sin| >= |cos| (decided on the integer angle, so it is exact).
+// the octants where |sin| >= |cos| (decided on the integer angle, so it is exact).  tau
+// holds the stored value: tau for f = 0, -tau for f = 1.
 struct RatioForm {
   DD rho, tau;
   int f;
@@ -235,9 +236,9 @@ RatioForm ratio_form(int64_t t, int64_t L) {
   const int64_t o = (8 * t) / L;
   RatioForm r;
   if (o == 1 || o == 2 || o == 5 || o == 6) {
-    r.f = 1;  // i rho (1 + i tau) = -rho tau + i rho
+    r.f = 1;  // i rho (1 + i tau) = -rho tau + i rho: tau = -re/im, stored negated
     r.rho = im;
-    r.tau = -(re / im);
+    r.tau = re / im;
   } else {
     r.f = 0;
     r.rho = re;
@@ -262,10 +263,9 @@ void ratio_values(int R, int64_t e, int64_t L, double* out) {
   if (R == 8) {
     DD c45, s45;
     sincos_octant(1, 1, &s45, &c45);  // cos(pi/4)
-    const double v[16] = {rd(w[1].tau), rd(w[2].tau), rd(w[3].tau), rd(w[4].tau), rd(w[5].tau),
-                          rd(w[6].tau), rd(w[7].tau), flags,       rd(w[4].rho), ratio(6, 2),
-                          rd(w[2].rho), ratio(5, 1),  ratio(7, 3), ratio(3, 1),  rd(w[1].rho),
-                          rd(w[1].rho * c45)};
+    const double v[16] = {rd(w[2].tau), rd(w[4].tau), rd(w[6].tau), flags,       rd(w[4].rho), ratio(6, 2),
+                          rd(w[2].rho), ratio(5, 1),  rd(w[1].tau), rd(w[5].tau), rd(w[3].tau), rd(w[7].tau),
+                          ratio(7, 3),  ratio(3, 1),  rd(w[1].rho), rd(w[1].rho * c45)};
     std::memcpy(out, v, sizeof v);
   } else if (R == 4) {
     const double v[8] = {rd(w[1].tau), rd(w[2].tau), rd(w[3].tau), flags, rd(w[2].rho), ratio(3, 1),
