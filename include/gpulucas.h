@@ -150,14 +150,14 @@ int gl_get_carry_state(gl_plan* plan, int32_t* digit_out, int8_t* hi_out); /* i_
  * iteration, or gl_get_carry_state, dices them with llintToIrrBal<n>
  * (IrrBaseBalanced.cu:52-110). */
 int gl_set_products(gl_plan* plan, const int64_t* ll, int64_t iterations);
-/* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */
 /* For callers that keep the state in host memory: loads the carry-save state (digit,
- * hi; N each, host buffers, pinned for full speed), runs `iters` iterations, and writes
- * the resulting state back, with one synchronisation for the whole call (the round-off
- * of these iterations is checked once, at the end).  digit_in/hi_in may alias
- * digit_out/hi_out. */
+ * hi; N each, host buffers), runs `iters` iterations, and writes the resulting state
+ * back, with one synchronisation for the whole call (the round-off of these iterations
+ * is checked once, at the end).  digit_in/hi_in may alias digit_out/hi_out; pinned
+ * buffers copy at the CPU link's full rate. */
 int gl_iterate_host(gl_plan* plan, const int32_t* digit_in, const int8_t* hi_in, int64_t iters,
                     int32_t* digit_out, int8_t* hi_out, gl_iter_report* report);
+/* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */
 int gl_set_carry_state(gl_plan* plan, const int32_t* digit, const int8_t* hi, int64_t iterations);
 
 /* addPseudoBalanced + rebalanceIrrIntSEQGPU + print_residue + zero test

@@ -225,6 +225,27 @@ def test_iterate_host_state_chain(gl, orc, p, N, mode):
         assert pl.res64() == orc.Exact(p).iterate(15).res64()
 
 
+@pytest.mark.parametrize("p,N,mode", [(1000003, 54432, 0), (100003, 5184, 1), (44497, 2048, 0)])
+def test_iterate_host_pinned_buffers(gl, orc, p, N, mode):
+    """Pinned host buffers, updated in place step after step: the same states as the
+    oracle."""
+    import ctypes
+
+    import torch
+    o = orc.IBDWT(p, N)
+    d0, h0 = o.state()
+    d = torch.from_numpy(np.ascontiguousarray(d0, np.int32)).pin_memory()
+    h = torch.from_numpy(np.ascontiguousarray(h0, np.int8)).pin_memory()
+    dp, hp = ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(h.data_ptr())
+    rep = gl.IterReport()
+    with gl.Plan(p, N, mode=mode) as pl:
+        for k in (1, 4, 1):
+            assert gl.lib.gl_iterate_host(pl._h, dp, hp, k, dp, hp, ctypes.byref(rep)) == 0
+            o.iterate(k)
+            d2, h2 = o.state()
+            assert (d.numpy() == d2).all() and (h.numpy() == h2).all()
+
+
 def test_bounded_wait_times_out_and_device_stays_usable(gl, orc):
     """A kernel waiting on a barrier that nothing completes gives up after its bound,
     the host reads GL_ERR_TIMEOUT, and the context keeps working (no trap, no hang)."""
