@@ -143,9 +143,32 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
   return out;
 }
 
+// Block size of the row pass (two lines of W points): from t0 (one thread per butterfly of
+// the largest-radix stage) up to kRowThreads, the smallest multiple of 32 that minimises
+// the stages' rounds of butterflies weighted by radix, so that a stage with more, smaller
+// butterflies (radix 3 after radix 8) does not leave most warps waiting at its barrier
+// while a few run one more round.  W = 576 (8, 8, 3, 3): 160 -> 192 threads.
+int row_threads(int W, const LinePlan& pw, int t0) {
+  int best = t0;
+  long best_cost = -1;
+  for (int t = t0; t <= kRowThreads; t += 32) {
+    long cost = 0;
+    for (int s = 0; s < pw.nst; ++s) {
+      const int R = pw.radix[s];
+      const int nb = 2 * W / R;
+      cost += (long)((nb + t - 1) / t) * R;
+    }
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = t;
+    }
+  }
+  return best;
+}
+
 // Layout for M: column length `force_h` (0: the model's best) with line plans whose
-// largest radix is rc (columns) / rr (rows); each line gets one thread per butterfly
-// of its largest-radix stage.
+// largest radix is rc (columns) / rr (rows); each column gets one thread per butterfly
+// of its largest-radix stage, each row pair row_threads().
 int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix,
                       bool ip = false, bool pf = false) {
   if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
@@ -172,7 +195,7 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
     return t < 64 ? 64 : (t > cap ? cap : t);
   };
   g->t_col = threads(g->H, rc, kMaxThreads);
-  g->t_row = threads(2 * g->W, rr, kRowThreads);
+  g->t_row = row_threads(g->W, g->pw, threads(2 * g->W, rr, kRowThreads));
   g->col_ip = 0;
   g->col_pf = 0;
   if (ip) {
