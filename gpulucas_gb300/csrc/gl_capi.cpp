@@ -91,7 +91,7 @@ constexpr double kBatchUnitOverhead = 2000.0;
 int stage_offsets(const LinePlan& lp, int* off);
 
 // Shared memory of a row-pass CTA: four line buffers (the pair, ping-pong) and the copy of
-// the length-W stage twiddles.
+// the length-W line DFT's stage values.
 size_t row_smem(int W, const LinePlan& pw) {
   int off[8];
   return (size_t)4 * padded_stride(W) * 16 + (size_t)stage_offsets(pw, off) * sizeof(DevCplx);
@@ -333,8 +333,9 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
       consider(ranked[i].second, 4, kMaxRadix, false);
       consider(ranked[i].second, kMaxRadix, 4, false);
       consider(ranked[i].second, 4, 4, false);
-      // radix-2 stages: the same FP64 work per point and bit in the layered form, twice
-      // the butterflies per stage, so twice the warps to hide FP64 latency on short lines
+      // radix-2 stages: a little more FP64 work per point and bit (3 against 2.75 for
+      // radix 4 in ratio form), twice the butterflies per stage, so twice the warps to hide
+      // FP64 latency on short lines
       consider(ranked[i].second, 2, 4, false);
       consider(ranked[i].second, 4, 2, false);
       consider(ranked[i].second, 2, 2, false);

@@ -10,8 +10,8 @@ namespace gl {
 
 // Line FFTs of the fused form use radices <= kMaxRadix and about kElemsPerThread
 // points per thread: a radix-8 butterfly keeps 8 complex values (32 registers) live,
-// so 3 CTAs of 256 threads fit an SM's registers.  With FMA-merged layered stages a
-// radix-8 stage costs the same 3 FP64 instructions per point and bit as a radix-16 one.
+// so 3 CTAs of 256 threads fit an SM's registers.  A twiddled radix-8 stage in ratio form
+// costs 2.75 FP64 instructions per point and bit, less than a layered radix-16 one (3).
 constexpr int kMaxRadix = 8;
 constexpr int kElemsPerThread = 8;
 constexpr int kMaxThreads = 256;

@@ -309,9 +309,9 @@ __global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 3) k_col_fwd(IterArgs a)
   col_fwd_body<FROM_STATE, NC, IP>(a, blockIdx.x);
 }
 
-// The row pass's stage twiddles (a few KB) are copied into shared memory behind the four
-// line buffers by one bulk copy, issued before the rows are loaded so the two overlap;
-// both DFTs of the pair, forward and inverse, then read twiddles from shared memory.
+// The row pass's stage values (17.4 KB at W = 576) are copied into shared memory behind
+// the four line buffers by one bulk copy, issued before the rows are loaded so the two
+// overlap; both DFTs of the pair, forward and inverse, then read them from shared memory.
 __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 .. H/2 */) {
   extern __shared__ cplx smem[];
   __shared__ alignas(8) uint64_t tw_bar;

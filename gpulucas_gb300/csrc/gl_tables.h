@@ -36,18 +36,21 @@ void weight_entry(int p, int N, int j, double inv_scale_den, double* A, double* 
 void twiddle_table(int64_t L, std::vector<HostCplx>& tw);
 HostCplx twiddle(int64_t t, int64_t L);
 
-// Stage-ordered twiddles of one Stockham line DFT of length L with the given radix
+// Stage-ordered values of one Stockham line DFT of length L with the given radix
 // sequence.  Stage s (span Ns, radix R, external twiddle w = w_L^(k L/(Ns R)) for
-// butterfly position k < Ns) stores its values v-major at off[s] + v*Ns + k, so lanes
-// with consecutive k read consecutive entries:
-//  - R a power of two: the layered radix-2 DIT needs, at level l = 1..log2 R, the
-//    values w^(R/2^l) * W_(2^l)^p for p < max(1, 2^(l-2)) (the other half are the same
-//    times +-i): v runs over (l=1,p=0), (l=2,p=0), (l=3,p=0..1), (l=4,p=0..3);
-//  - R odd: w^q for q = 1..R-1.
+// butterfly position k < Ns) stores its 16-byte slots v-major at off[s] + v*Ns + k, so
+// lanes with consecutive k read consecutive slots:
+//  - R = 8, 4, 3: the ratio form of w^q = i^f rho_q (1 + i tau_q) (8, 4, 4 slots of two
+//    doubles: tau, ratios of rho, flags; the order is the device butterflies', ratio_r8,
+//    ratio_r4, ratio_r3 in gl_device.cuh);
+//  - R = 2, 16: the layered radix-2 DIT needs, at level l = 1..log2 R, the values
+//    w^(R/2^l) * W_(2^l)^p for p < max(1, 2^(l-2)) (the other half are the same times
+//    +-i): v runs over (l=1,p=0), (l=2,p=0), (l=3,p=0..1), (l=4,p=0..3);
+//  - R = 5, 7: w^q for q = 1..R-1.
 // The first stage (Ns = 1) needs no table.  Returns the table (at least one entry)
 // and fills off[] (offset of each stage).
 void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx>& tw, int* off);
-// number of stored values per butterfly position for a stage of radix R
+// number of stored 16-byte slots per butterfly position for a stage of radix R
 int stage_values(int R);
 
 // -(1 + w_M^k)/4 from double-double cos/sin, rounded once: the coefficient of the

@@ -68,7 +68,7 @@ def test_describe_layouts(gl, p, N, mode):
         assert info.cols_per_cta == 1
         ls = lambda L: L + L // 16 + 1  # noqa: E731  padded line stride
         assert info.smem_col == 2 * ls(info.fft_h) * 16 <= 110 * 1024
-        # four line buffers plus the row pass's stage twiddles, copied in by one bulk copy
+        # four line buffers plus the row pass's stage values, copied in by one bulk copy
         # slots per butterfly position: radix 8, 4, 3 in ratio form (8, 4, 4), radix 2 one
         # complex value, 5 and 7 one per twiddled input
         values = lambda r: {2: 1, 3: 4, 4: 4, 8: 8, 16: 8}.get(r, r - 1)  # noqa: E731
