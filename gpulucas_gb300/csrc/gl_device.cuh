@@ -362,11 +362,6 @@ GL_HD void dft(cplx* x) {
 //   R = 3: tau1, tau2, rho2/rho1, flags, rho1, rho1/2, rho1 sin(2pi/3), 0
 // flags: bit q = f of w^q, held as the bit pattern of the double.
 // ---------------------------------------------------------------------------
-template <int R>
-GL_HD constexpr bool ratio_stage() {
-  return R == 3 || R == 4 || R == 8;
-}
-
 // Sign of x flipped when f == 1, by an integer instruction on the high word.  Inline PTX
 // keeps the compiler from turning a sign-bit XOR back into an FP64 negation, which it
 // would issue as a DADD when the negated value feeds a select.

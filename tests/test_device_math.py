@@ -152,3 +152,63 @@ def test_line_dft_through_stage_tables(hc, radices, sign):
     y = buf[0::2] + 1j * buf[1::2]
     ref = np.fft.fft(x) if sign < 0 else np.fft.ifft(x) * L
     assert np.abs(y - ref).max() <= 2e-15 * np.abs(ref).max()
+
+
+def _ratio_twiddles(R, d):
+    """w^q, q = 1..R-1, decoded from one position's stored doubles of a ratio-form stage:
+    w^q = i^f rho_q (1 + i tau_q), tau stored negated where f = 1, rho from the ratios."""
+    flags = int(np.array([d[{8: 3, 4: 3, 3: 3}[R]]], np.float64).view(np.int64)[0])
+    if R == 8:
+        tau = {2: d[0], 4: d[1], 6: d[2], 1: d[8], 5: d[9], 3: d[10], 7: d[11]}
+        rho = {1: d[14], 2: d[6], 4: d[4]}
+        rho[3] = d[13] * rho[1]
+        rho[5] = d[7] * rho[1]
+        rho[6] = d[5] * rho[2]
+        rho[7] = d[12] * rho[3]
+        assert d[15] == pytest.approx(rho[1] / np.sqrt(2), rel=1e-15)
+    elif R == 4:
+        tau = {1: d[0], 2: d[1], 3: d[2]}
+        rho = {1: d[6], 2: d[4]}
+        rho[3] = d[5] * rho[1]
+    else:
+        tau = {1: d[0], 2: d[1]}
+        rho = {1: d[4], 2: d[2] * d[4]}
+        assert d[5] == rho[1] / 2 and d[6] == pytest.approx(rho[1] * np.sin(2 * np.pi / 3), rel=1e-15)
+    out = {}
+    for q in range(1, R):
+        f = (flags >> q) & 1
+        t = -tau[q] if f else tau[q]
+        assert abs(t) <= 1.0 and abs(rho[q]) >= np.sqrt(0.5) * (1 - 1e-15)
+        out[q] = (1j ** f) * rho[q] * (1 + 1j * t)
+    return out
+
+
+@pytest.mark.parametrize("radices", [[8, 8, 3, 3], [8, 8, 8, 4], [4, 4, 3], [3, 8, 4]])
+def test_ratio_stage_values_decode_to_twiddles(hc, radices):
+    """The stored ratio-form values of every position of every twiddled radix-8/4/3 stage
+    give back w^q = exp(-2 pi i k q / (Ns R)) to a few ulps, with |tau| <= 1 (the bound
+    allows for the decoding's chained ratios and numpy's own rounding of the angle; a value
+    in the wrong slot is off by O(1))."""
+    f = hc.hc_stage_twiddles
+    f.argtypes = [ctypes.c_int, np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"), ctypes.c_int,
+                  ctypes.c_void_p, np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")]
+    f.restype = ctypes.c_int
+    L = int(np.prod(radices))
+    rad = np.array(radices, np.int32)
+    off = np.zeros(16, np.int32)
+    n = f(L, rad, len(radices), None, off)
+    tab = np.empty(2 * n)
+    assert f(L, rad, len(radices), tab.ctypes.data, off) == n
+    slots = {8: 8, 4: 4, 3: 4}
+    Ns = 1
+    for s, R in enumerate(radices):
+        if Ns > 1 and R in slots:
+            for k in range(Ns):
+                d = np.empty(2 * slots[R])
+                for v in range(slots[R]):
+                    d[2 * v:2 * v + 2] = tab[2 * (off[s] + v * Ns + k):2 * (off[s] + v * Ns + k) + 2]
+                w = _ratio_twiddles(R, d)
+                for q, val in w.items():
+                    ref = np.exp(-2j * np.pi * k * q / (Ns * R))
+                    assert abs(val - ref) <= 1.5e-15, (s, R, k, q, val, ref)
+        Ns *= R
