@@ -82,6 +82,21 @@ def test_describe_layouts(gl, p, N, mode):
         assert 64 <= info.threads_row <= 256 and info.threads_row % 32 == 0
 
 
+def test_row_block_balances_stages(gl):
+    """A row CTA (two lines of W points) gets the smallest block that minimises the stages'
+    rounds weighted by radix: W = 576 (8, 8, 3, 3) runs 192 threads, so its radix-3 stages
+    (384 butterflies) take two even rounds."""
+    info = gl.describe(43112609, 2359296)
+    rw = [r for r in info.radix_w if r]
+    assert info.fft_w == 576 and rw == [8, 8, 3, 3] and info.threads_row == 192
+    for p, N in [(2976221, 163840), (1000003, 54432), (300007, 15360)]:
+        info = gl.describe(p, N)
+        t = info.threads_row
+        rw = [r for r in info.radix_w if r]
+        cost = lambda t: sum(-(-2 * info.fft_w // r // t) * r for r in rw)  # noqa: E731
+        assert all(cost(t) <= cost(u) for u in range(64, 257, 32) if u >= t)
+
+
 def test_plan_without_gpu_reports_status(gl):
     import torch
     if torch.cuda.is_available():
