@@ -1,7 +1,7 @@
 // gl_residue.cu -- end-of-run normalisation and Res64 on the device.
 //
 // The reference does this serially: addPseudoBalanced + rebalanceIrrIntSEQGPU, one
-// thread walking all N words with a balanced carry (inner.cu:117-169, about 0.5 s per call
+// thread walking all N words with a balanced carry (IrrBaseBalanced.cu:117-169, about 0.5 s per call
 // at 26M-range exponents), then print_residue on the host borrows the digits
 // non-negative and packs the low 64 bits (gpuLucas.cu:1288-1352).  Both walks are carry
 // chains whose carry takes few values, so each word is a function from carry-in to

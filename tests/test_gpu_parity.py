@@ -71,7 +71,7 @@ def _carry_states(orc, p, N, rng):
 @pytest.mark.parametrize("mode", [0, 1], ids=["fused", "plain"])
 def test_device_residue_matches_oracle(gl, orc, p, N, mode):
     """The device normalisation (balanced rebalance, canonical digits, Res64, zero test)
-    against the oracle's restatement of rebalanceIrrIntSEQGPU (inner.cu:133-169) and
+    against the oracle's restatement of rebalanceIrrIntSEQGPU (IrrBaseBalanced.cu:133-169) and
     print_residue (gpuLucas.cu:1288-1352) on arbitrary carry-save states.  N = 2359296
     spans 1152 blocks of the scan, more than one pass of the one-block scan."""
     rng = np.random.default_rng(N + mode)
