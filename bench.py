@@ -201,6 +201,34 @@ def run_reference(args, world: int, rank: int):
     print(json.dumps(line), flush=True)
 
 
+def ref_cufft_leg(dev: int) -> dict:
+    """Baseline leg: the reference program itself (gpuLucas.cu with cuFFT, built for sm_103a
+    by oracle/build_ref.py) on the same GPU, non-verbose, timed by its own checkpoint lines
+    (cudaEvents between checkpoints, one checkpoint write per interval; the second interval
+    is reported, the first includes cuFFT's first calls)."""
+    try:
+        from oracle import refrun
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"oracle import failed: {e}"}
+    if not refrun.available():
+        return {"unavailable": "reference program not built (no reference sources staged)"}
+    out = {"program": "gpuLucas -d DEV -f N -c K p (reference sources, patched only for safety and CUDA 13; "
+                      "cuFFT D2Z/Z2D + 5 kernels per iteration)",
+           "timing": "ms/iter printed at its 2nd checkpoint line: wall time of K iterations between two "
+                     "checkpoints by cudaEvents, one checkpoint write included; L2 warm (continuous run)"}
+    for name, p, N, every in (("c2", 2976221, 163840, 20000), ("c3", P3, N3, 4000)):
+        try:
+            r = refrun.run(p, N, every=every, checkpoints=2, verbose=False, timeout=600, device=dev)
+            ms = r.ms_per_iter(-1)
+            out[name] = {"p": p, "N": N, "iterations_per_interval": every, "ms_per_iter": ms,
+                         "iter_s": 1e3 / ms, "ms_per_iter_first_interval": r.ms_per_iter(0),
+                         "wall_s": r.wall_s}
+        except Exception as e:
+            out[name] = {"unavailable": f"{type(e).__name__}: {str(e).splitlines()[0][:200]}"}
+    out["c1"] = {"unavailable": "refused by the reference: p/N = 21 (gpuLucas.cu:327-331)"}
+    return out
+
+
 def rate(gl, p, N, mode, seconds=0.4, device=0):
     """Continuous (L2-warm) iterations/s of one form, for the by-length table."""
     with gl.Plan(p, N, mode=mode, device=device, check_every=1 << 30) as pl:
@@ -316,14 +344,66 @@ def run_ours(args, world: int, rank: int, local: int):
             pl_, ep = rate(gl, p, N, gl.MODE_PLAIN, device=dev)
             by[name] = {"p": p, "N": N, "fused_iter_s": f, "plain_iter_s": pl_, "fused_over_plain": f / pl_,
                         "fused_max_roundoff": ef, "plain_max_roundoff": ep, "l2": "warm (continuous run)"}
+        if args.ref_cufft:
+            ref = ref_cufft_leg(dev)
+            line["ref_cufft"] = ref
+            for name in ("c2", "c3"):
+                if "iter_s" in ref.get(name, {}):
+                    by[name]["ref_cufft_iter_s"] = ref[name]["iter_s"]
+                    by[name]["fused_over_ref_cufft"] = by[name]["fused_iter_s"] / ref[name]["iter_s"]
+            if "iter_s" in ref.get("c3", {}):
+                line["value_over_ref_cufft"] = value / world / ref["c3"]["iter_s"]
         line["by_fft_length"] = by
         line["cpu_baseline"] = cpu_baseline(P3, N3)
         if args.batched_iters > 0:
             line["batched"] = batched_leg(gl, dev, args.batched_iters)
         if args.serve_window > 0:
             line["served"] = served_leg(gl, dev, args.serve_window)
+    if world > 1 and args.batched_iters > 0:
+        sb = sharded_batched_leg(gl, dev, args.batched_iters, rank, world)
+        if rank == 0:
+            line["batched"] = sb
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def sharded_batched_leg(gl, dev: int, iters: int, rank: int, world: int) -> dict:
+    """The batched configuration sharded over the ranks (one GPU each): each rank advances
+    the tests shard.partition gives it (by modelled FP64 work) in its own batch; the
+    records are gathered once at the end (all_gather_object, no data-path collective).
+    tests/h = all tests / the slowest rank's device time."""
+    import torch.distributed as dist
+
+    from gpulucas_gb300 import shard, workloads
+    ps = workloads.batch_exponents()
+    Ns = [gl.smallest_signal_size(p, 19.5) for p in ps]
+    mine = shard.partition([shard.flop_alg(n) * iters for n in Ns], world)[rank]
+    b = gl.Batch([ps[i] for i in mine], [Ns[i] for i in mine], device=dev, check_every=1000) if mine else None
+    barrier(world)
+    ms = b.iterate(iters, check=False).ms if b else 0.0
+    recs = []
+    if b:
+        for j, i in enumerate(mine):
+            r, st = b.result(j)
+            recs.append((i, r.res64, st, r.max_roundoff))
+        b.close()
+    t = dist_max(ms * 1e-3, world)
+    parts = [None] * world
+    dist.all_gather_object(parts, recs)
+    merged = sorted((x for part in parts for x in part), key=lambda x: x[0])
+    if [x[0] for x in merged] != list(range(len(ps))):
+        raise RuntimeError("sharded batch lost or duplicated tests")
+    return {
+        "workload": f"{len(ps)} primes drawn uniformly from [1e5, 3e6] (numpy default_rng(4)), smallest "
+                    f"7-smooth even N with p/N <= 19.5, {iters} iterations from S0=4, sharded by test over "
+                    f"{world} ranks",
+        "tests": len(ps), "iterations": iters, "ranks": world, "scaling": "strong (fixed 256-test batch)",
+        "tests_per_rank": [len(p) for p in shard.partition([shard.flop_alg(n) * iters for n in Ns], world)],
+        "seconds": t, "tests_per_h": len(ps) / t * 3600.0,
+        "tflops_alg": sum(flop_alg(N) for N in Ns) * iters / t / 1e12,
+        "max_roundoff": max(x[3] for x in merged), "failed": sum(1 for x in merged if x[2] != 0),
+        "gpu_launches_per_rank": 3 * iters,
+    }
 
 
 def batched_leg(gl, dev: int, iters: int) -> dict:
@@ -420,6 +500,8 @@ def main():
     ap.add_argument("--batched-iters", type=int, default=10000,
                     help="iterations of the 256-test batched leg (0: skip)")
     ap.add_argument("--serve-window", type=int, default=64, help="requests in the served leg (0: skip)")
+    ap.add_argument("--ref-cufft", type=int, default=1,
+                    help="1: time the reference cuFFT program on the same GPU (baseline leg); 0: skip")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

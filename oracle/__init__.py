@@ -12,6 +12,10 @@ Three independent implementations:
 * ``Exact`` -- ``exact_oracle.c``: exact S^2 - 2 mod 2^p - 1 by a number-theoretic
   transform, no floating point.
 * ``lucas_lehmer_int`` -- pure Python integers, for small p.
+
+Beside them, ``refrun`` runs the reference program itself (gpuLucas.cu with cuFFT,
+compiled for the GPU by ``build_ref.py`` into the git-ignored ``oracle/_ref/``) and reads
+its Res64, timings and checkpointed state.
 """
 from __future__ import annotations
 
@@ -31,6 +35,16 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH):
         subprocess.run(["make", "-C", _HERE, "-s"], check=True)
     return _LIB_PATH
+
+
+def build_ref(force: bool = False):
+    """Stage and compile the reference gpuLucas program (oracle/build_ref.py); returns its
+    path, or None when neither the reference checkout nor a staged copy is present."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gl_oracle_build_ref", os.path.join(_HERE, "build_ref.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
 
 
 def lib():
