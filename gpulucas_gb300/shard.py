@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import heapq
 import math
+import os
 from typing import Callable, Sequence
 
 
@@ -32,16 +33,29 @@ def partition(costs: Sequence[float], world: int) -> list[list[int]]:
     return [sorted(x) for x in out]
 
 
+def local_device(rank: int, device_count: int | None = None) -> int:
+    """The GPU of this rank on its node: LOCAL_RANK when the launcher sets it (torchrun
+    does), else the global rank; modulo the visible device count when it is known."""
+    dev = int(os.environ.get("LOCAL_RANK", rank))
+    if device_count:
+        dev %= device_count
+    return dev
+
+
 def run_sharded(ps: Sequence[int], Ns: Sequence[int], iterations: int, rank: int, world: int,
-                runner: Callable[[list[int], list[int], int], list[tuple[int, int, float]]],
-                gather: Callable[[object], list[object]] | None = None) -> list[tuple[int, int, float]] | None:
-    """Run this rank's share; `runner(ps, Ns, iterations)` returns one (res64, status,
-    max_roundoff) per test.  With `gather` (an all_gather_object), rank 0 returns the
-    records of all tests in input order, others None; without it, this rank's own
-    (index, res64, status, max_roundoff) records."""
+                runner: Callable[[list[int], list[int], int, int], list[tuple[int, int, float]]],
+                gather: Callable[[object], list[object]] | None = None,
+                device: int | None = None) -> list[tuple[int, int, float]] | None:
+    """Run this rank's share on `device` (default: local_device(rank));
+    `runner(ps, Ns, iterations, device)` returns one (res64, status, max_roundoff) per
+    test.  With `gather` (an all_gather_object), rank 0 returns the records of all tests
+    in input order, others None; without it, this rank's own (index, res64, status,
+    max_roundoff) records."""
+    if device is None:
+        device = local_device(rank)
     costs = [flop_alg(n) * iterations for n in Ns]
     mine = partition(costs, world)[rank]
-    res = runner([ps[i] for i in mine], [Ns[i] for i in mine], iterations) if mine else []
+    res = runner([ps[i] for i in mine], [Ns[i] for i in mine], iterations, device) if mine else []
     records = [(i,) + tuple(r) for i, r in zip(mine, res)]
     if gather is None:
         return records
@@ -54,8 +68,8 @@ def run_sharded(ps: Sequence[int], Ns: Sequence[int], iterations: int, rank: int
     return [tuple(r[1:]) for r in merged]
 
 
-def gpu_runner(ps: list[int], Ns: list[int], iterations: int, device: int = 0):
-    """Runner over one gl_batch on `device`."""
+def gpu_runner(ps: list[int], Ns: list[int], iterations: int, device: int):
+    """Runner over one gl_batch on `device` (this rank's GPU)."""
     import gpulucas_gb300 as gl
     with gl.Batch(ps, Ns, device=device) as b:
         b.iterate(iterations, check=False)

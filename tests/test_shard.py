@@ -53,7 +53,7 @@ def test_serving_requests_shape():
     assert all(workloads.is_prime(r.p) and 100_000 <= r.p <= 50_000_100 for r in reqs)
 
 
-def _oracle_runner(ps, Ns, iterations):
+def _oracle_runner(ps, Ns, iterations, device=0):
     import oracle
     return [(oracle.Exact(p).iterate(iterations).res64(), 0, 0.0) for p in ps]
 
@@ -78,12 +78,20 @@ def _rank_main(rank, world, port, ps, Ns, iters, out_path):
         dist.all_gather_object(parts, obj)
         return parts
 
-    res = sh.run_sharded(ps, Ns, iters, rank, world, _oracle_runner, gather)
+    devices = []
+
+    def runner(ps_, Ns_, it, device):
+        devices.append(device)
+        return _oracle_runner(ps_, Ns_, it, device)
+
+    os.environ["LOCAL_RANK"] = str(rank)
+    res = sh.run_sharded(ps, Ns, iters, rank, world, runner, gather)
+    seen = gather(devices)
     dist.barrier()
     dist.destroy_process_group()
     if rank == 0:
         with open(out_path, "wb") as f:
-            pickle.dump(res, f)
+            pickle.dump((res, seen), f)
 
 
 def test_sharded_run_two_gloo_ranks(tmp_path):
@@ -97,5 +105,30 @@ def test_sharded_run_two_gloo_ranks(tmp_path):
     mp.start_processes(_rank_main, args=(2, _free_port(), ps, Ns, iters, out), nprocs=2, join=True,
                        start_method="spawn")
     with open(out, "rb") as f:
-        res = pickle.load(f)
+        res, seen = pickle.load(f)
     assert res == _oracle_runner(ps, Ns, iters)
+    # each rank ran its share on its own device (LOCAL_RANK), not all on device 0
+    assert seen == [[0], [1]]
+
+
+def test_local_device(monkeypatch):
+    monkeypatch.delenv("LOCAL_RANK", raising=False)
+    assert shard.local_device(3) == 3 and shard.local_device(9, 8) == 1
+    monkeypatch.setenv("LOCAL_RANK", "5")
+    assert shard.local_device(13) == 5 and shard.local_device(13, 4) == 1
+
+
+@pytest.mark.gpu
+def test_sharded_gpu_runner_one_rank_matches_golden(gl):
+    """run_sharded with the GPU runner on this process's GPU (world 1, no gather): the
+    batched configuration's golden exponents after 10000 iterations."""
+    import json
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "res64_batch.json")) as f:
+        golden = json.load(f)
+    ps = [e["p"] for e in golden]
+    Ns = [e["N"] for e in golden]
+    recs = shard.run_sharded(ps, Ns, 10000, 0, 1, shard.gpu_runner, device=0)
+    assert [r[0] for r in recs] == list(range(len(ps)))
+    for (i, res64, st, err), e in zip(recs, golden):
+        assert st == 0 and err < 0.4
+        assert f"{res64:016x}" == e["res64"], e["p"]
