@@ -218,10 +218,9 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
 }
 
 int choose_plain_geom(int M, PlainGeom* g) {
-  std::vector<int> r = radix_plan(M, 4);
-  if (r.empty() || r.size() > 40) return GL_ERR_SIZE;
-  g->nst = (int)r.size();
-  for (int i = 0; i < g->nst; ++i) g->radix[i] = r[i];
+  const int nst = radix_plan_into(M, 4, g->radix, 40);
+  if (nst <= 0) return GL_ERR_SIZE;
+  g->nst = nst;
   g->threads = 256;
   return GL_OK;
 }

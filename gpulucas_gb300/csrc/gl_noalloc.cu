@@ -61,11 +61,10 @@ struct DeviceSlot {
 static DeviceSlot g_slots[kMaxDevices];
 static std::mutex g_mutex;  // host-side state: staging buffers and the slots
 
-int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
-
-// Fill the host staging tables for (p, N) exactly as a GL_MODE_PLAIN plan does.
+// Fill the host staging tables for (p, N) with the entry helpers a GL_MODE_PLAIN plan's
+// tables are built from (gl_tables.cpp), so the two cannot drift apart.
 void build_tables(int p, int N) {
-  const int M = N / 2, LO = p / N;
+  const int M = N / 2;
   for (int k = 0; k < M; ++k) {
     const HostCplx w = twiddle(k, M);
     const HostCplx c = pair_coeff(k, M);
@@ -73,15 +72,7 @@ void build_tables(int p, int N) {
     h_pair[k] = {c.re, c.im};
   }
   for (int j = 0; j < N; ++j) weight_entry(p, N, j, (double)M, &h_A[j], &h_Ainv[j]);
-  for (int j = 0; j < N; ++j) {
-    unsigned char v = 0;
-    for (int b = 0; b < 8; ++b) {
-      const int k = ((j - b) % N + N) % N;
-      const int64_t bits = ceil_div((int64_t)p * (k + 1), N) - ceil_div((int64_t)p * k, N);
-      v |= (unsigned char)((bits != LO ? 1 : 0) << b);
-    }
-    h_flags[j] = v;
-  }
+  for (int j = 0; j < N; ++j) h_flags[j] = word_flags(p, N, j);
 }
 
 }  // namespace
@@ -94,23 +85,19 @@ extern "C" int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* l
   if (!ll_in || !ll_out || iters < 0) return GL_ERR_ARG;
   if (p < 3 || N < 16 || (N & 1) || N > p) return GL_ERR_ARG;
   if (N > kNoAllocMaxN) return GL_ERR_TOO_LARGE;
+  {
+    // the same buffer is fine; buffers that share only part of their words are not
+    const int64_t* out_c = ll_out;
+    if (out_c != ll_in && out_c < ll_in + N && ll_in < out_c + N) return GL_ERR_ARG;
+  }
   const int n = slice_depth(p, N);
   if (n < 0) return GL_ERR_RATIO;
   const int M = N / 2;
   PlainGeom pg{};
-  {
-    // radices of the plain form (<= 4), as a GL_MODE_PLAIN plan picks them
-    int m = M, ns = 0;
-    const int order[5] = {4, 2, 3, 5, 7};
-    for (int r : order)
-      while (m % r == 0 && ns < 40) {
-        pg.radix[ns++] = r;
-        m /= r;
-      }
-    if (m != 1) return GL_ERR_SIZE;
-    pg.nst = ns;
-    pg.threads = 256;
-  }
+  // radices of the plain form (<= 4), by the helper a GL_MODE_PLAIN plan uses
+  pg.nst = radix_plan_into(M, 4, pg.radix, 40);
+  if (pg.nst <= 0) return GL_ERR_SIZE;
+  pg.threads = 256;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GL_ERR_CUDA;
@@ -118,11 +105,16 @@ extern "C" int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* l
 
   std::lock_guard<std::mutex> lock(g_mutex);
   DeviceSlot& slot = g_slots[dev];
-  if (!slot.base) {
-    // once per device, with that device current
+  {
+    // The array's device address, looked up with this device current on every call (the
+    // lookup allocates nothing).  If it moved -- the context was reset and the module
+    // loaded again -- the tables the slot remembers are gone too.
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return GL_ERR_CUDA;
-    slot.base = static_cast<unsigned char*>(ptr);
+    if (static_cast<unsigned char*>(ptr) != slot.base) {
+      slot.base = static_cast<unsigned char*>(ptr);
+      slot.p = slot.N = 0;
+    }
   }
   unsigned char* base = slot.base;
   if (slot.p != p || slot.N != N) {

@@ -131,20 +131,25 @@ int slice_depth(int p, int N) {
   return 6;
 }
 
-void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>& flags) {
+int word_bits(int p, int N, int j) {
+  return (int)(ceil_div_pos((int64_t)p * (j + 1), N) - ceil_div_pos((int64_t)p * j, N));
+}
+
+uint8_t word_flags(int p, int N, int j) {
   const int LO = p / N;
+  uint8_t v = 0;
+  for (int b = 0; b < 8; ++b) {
+    const int k = ((j - b) % N + N) % N;
+    v |= (uint8_t)((word_bits(p, N, k) != LO ? 1 : 0) << b);
+  }
+  return v;
+}
+
+void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>& flags) {
   bits.resize(N);
   flags.resize(N);
-  for (int j = 0; j < N; ++j)
-    bits[j] = (int32_t)(ceil_div_pos((int64_t)p * (j + 1), N) - ceil_div_pos((int64_t)p * j, N));
-  for (int j = 0; j < N; ++j) {
-    uint8_t v = 0;
-    for (int b = 0; b < 8; ++b) {
-      int k = ((j - b) % N + N) % N;
-      v |= (uint8_t)((bits[k] != LO ? 1 : 0) << b);
-    }
-    flags[j] = v;
-  }
+  for (int j = 0; j < N; ++j) bits[j] = (int32_t)word_bits(p, N, j);
+  for (int j = 0; j < N; ++j) flags[j] = word_flags(p, N, j);
 }
 
 void weight_entry(int p, int N, int j, double inv_scale_den, double* A, double* Ainv) {
@@ -319,27 +324,25 @@ void stage_twiddles(int L, const std::vector<int>& radices, std::vector<HostCplx
   }
 }
 
+int radix_plan_into(int n, int max_radix, int* out, int cap) {
+  if (n <= 0) return -1;
+  int m = n, count = 0;
+  const int radices[7] = {16, 8, 4, 2, 3, 5, 7};
+  for (int q : radices) {
+    if (q <= 16 && (q & (q - 1)) == 0 && q > max_radix) continue;  // power-of-two cap
+    while (m % q == 0) {
+      if (count == cap) return -1;
+      out[count++] = q;
+      m /= q;
+    }
+  }
+  return m == 1 ? count : -1;
+}
+
 std::vector<int> radix_plan(int n, int max_radix) {
-  std::vector<int> r;
-  if (n <= 0) return r;
-  int m = n;
-  const int pow2[4] = {16, 8, 4, 2};
-  for (int q : pow2) {
-    if (q > max_radix) continue;
-    while (m % q == 0) {
-      r.push_back(q);
-      m /= q;
-    }
-  }
-  const int odd[3] = {3, 5, 7};
-  for (int q : odd) {
-    while (m % q == 0) {
-      r.push_back(q);
-      m /= q;
-    }
-  }
-  if (m != 1) r.clear();
-  return r;
+  int buf[64];
+  const int count = radix_plan_into(n, max_radix, buf, 64);
+  return count < 0 ? std::vector<int>() : std::vector<int>(buf, buf + count);
 }
 
 }  // namespace gl

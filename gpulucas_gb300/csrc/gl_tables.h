@@ -23,6 +23,9 @@ int slice_depth(int p, int N);
 // exact integer arithmetic); flags[j] bit i = word (j-i) mod N has LO+1 bits, i < 8
 // (computeBitsPerWordVectors, gpuLucas.cu:700-714).
 void word_tables(int p, int N, std::vector<int32_t>& bits, std::vector<uint8_t>& flags);
+// One entry of each: bits[j] and flags[j] of word_tables (no containers).
+int word_bits(int p, int N, int j);
+uint8_t word_flags(int p, int N, int j);
 
 // A[j] = 2^(ceil(jp/N) - jp/N) and Ainv[j] = 2^-(ceil(jp/N) - jp/N) * scale, computed in
 // double-double and rounded once (computeWeightVectors, gpuLucas.cu:673-686, uses
@@ -57,8 +60,12 @@ int stage_values(int R);
 // real-signal square V_k = U_k^2 + c_k (U_k - conj(U_{M-k}))^2.
 HostCplx pair_coeff(int64_t k, int64_t M);
 
-// factor n into the allowed radices (16, 8, 4, 2, 3, 5, 7), largest first; empty if
-// n has another prime factor.
+// factor n into the allowed radices (16, 8, 4, 2, 3, 5, 7; powers of two up to
+// max_radix), largest power of two first, then 3, 5, 7; empty if n has another prime
+// factor.
 std::vector<int> radix_plan(int n, int max_radix);
+// The same into out[0..cap): returns the number of stages, or -1 if n has another prime
+// factor or needs more than cap stages.
+int radix_plan_into(int n, int max_radix, int* out, int cap);
 
 }  // namespace gl

@@ -356,13 +356,16 @@ int gl_server_destroy(gl_server* server);
  * runs `iters` LL iterations (the plain form, bit-identical products to a
  * GL_MODE_PLAIN plan) on the current device and `stream` (NULL = default stream),
  * from the products ll_in to the products ll_out (N int64 each, device memory owned
- * by the caller, natural word order; they may be the same buffer), and stores the
- * maximum round-off in *max_roundoff.  It allocates nothing: its work arrays, tables
- * and status word live in a static device array sized for N <= 65536 (about 3.3 MiB,
- * held on every GPU that loads the library until exit); larger N returns
- * GL_ERR_TOO_LARGE.  The first call on a device looks up that array's address;
- * make it before any stream capture on that device.  All calls share the array, so
- * calls that overlap on the GPU race; the host side is serialised by a lock.
+ * by the caller, natural word order; they may be the same buffer, but buffers that
+ * overlap only in part return GL_ERR_ARG), and stores the maximum round-off in
+ * *max_roundoff.  It allocates nothing: its work arrays, tables and status word live in
+ * a static device array sized for N <= 65536 (about 3.3 MiB, held on every GPU that
+ * loads the library until exit); larger N returns GL_ERR_TOO_LARGE.  The first call on
+ * a device sets up that device (looks up the array's address and uploads the test's
+ * tables); make it before any stream capture on that device.  The call is synchronous:
+ * it returns after `stream` has finished the iterations.  All calls share the array and
+ * would race if they overlapped on the GPU; a lock held until the stream has finished
+ * keeps the calls of one process from overlapping.
  * Returns GL_ERR_ROUNDOFF at round-off >= 0.4 and GL_ERR_OVERFLOW as gl_iterate. */
 int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* ll_out, int64_t iters,
                        double* max_roundoff, void* stream);

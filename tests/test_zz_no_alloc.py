@@ -67,3 +67,17 @@ def test_noalloc_rejects_sizes_above_limit(gl):
                                    ctypes.byref(err), None)
     assert rc == gl.GL_ERR_TOO_LARGE
     assert "65536" in gl.error_string(rc)
+
+
+def test_noalloc_rejects_partly_overlapping_buffers(gl):
+    """ll_in and ll_out may be the same buffer, but not overlap in part (the copy between
+    them would be undefined)."""
+    import torch
+    N = 2048
+    d = torch.zeros(2 * N, dtype=torch.int64, device="cuda")
+    err = ctypes.c_double()
+    base = d.data_ptr()
+    for shift in (1, N - 1):
+        rc = gl.lib.gl_iterate_noalloc(44497, N, ctypes.c_void_p(base), ctypes.c_void_p(base + 8 * shift), 1,
+                                       ctypes.byref(err), None)
+        assert rc == gl.GL_ERR_ARG, shift
