@@ -119,7 +119,7 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
   for (int H = 2; H <= M / 2; ++H) {
     if (M % H) continue;
     const int W = M / H;
-    if (W < 2) continue;
+    if (W < 4) continue;  // the forward column pass finds the words below a column with one wrap
     LinePlan a, b;
     if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
     const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = row_smem(W, a);
@@ -170,7 +170,7 @@ int row_threads(int W, const LinePlan& pw, int t0) {
 // largest radix is rc (columns) / rr (rows); each column gets one thread per butterfly
 // of its largest-radix stage, each row pair row_threads().
 int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix,
-                      bool ip = false, bool pf = false) {
+                      bool ip = false, bool pf = false, bool ws = false) {
   if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
   int bestH = 0;
   for (const auto& c : ranked_layouts(M, sms))
@@ -198,7 +198,8 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   g->t_row = row_threads(g->W, g->pw, threads(2 * g->W, rr, kRowThreads));
   g->col_ip = 0;
   g->col_pf = 0;
-  if (ip) {
+  g->col_ws = 0;
+  if (ip || ws) {
     // in place: every column stage has at most (8 / R for radix R = 2^k, 1 for odd R)
     // butterflies per thread, held in registers across the stage's first barrier
     for (int s = 0; s < g->ph.nst; ++s) {
@@ -208,6 +209,14 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
     }
     g->col_ip = 1;
     g->sm_col = g->sm_cinv = (size_t)g->ls_col * 16;
+    if (ws) {
+      // two columns per CTA: two in-place line buffers, no prefetch area
+      if (g->W < 2 || g->t_col != kMaxThreads) return GL_ERR_SIZE;
+      g->col_ws = 1;
+      g->sm_col = g->sm_cinv = (size_t)2 * g->ls_col * 16;
+      if (g->sm_col > (size_t)kMaxDynSmem) return GL_ERR_SIZE;
+      return GL_OK;
+    }
     if (pf) {
       if (g->H % 8) return GL_ERR_SIZE;  // bulk copies of 2H bytes must be 16-byte multiples
       g->col_pf = 1;
@@ -239,9 +248,10 @@ int stage_offsets(const LinePlan& lp, int* off) {
 
 // Device time of one fused iteration with column length H, measured on zero-filled
 // buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
-double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, int n, int sms, int iters, cudaStream_t s) {
+double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, bool ws, int n, int sms, int iters,
+                   cudaStream_t s) {
   FusedGeom g{};
-  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip, pf) != GL_OK) return -1.0;
+  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip, pf, ws) != GL_OK) return -1.0;
   const int N = 2 * M;
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
@@ -286,10 +296,14 @@ double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, int n, int sm
 // model are timed and the fastest kept, once per (M, SM count) per process.  Below
 // 2^17 complex points the lines are too short to fill the GPU with one thread per
 // radix-8 butterfly, so the three best lengths are also timed with radix-4 and radix-2
-// caps.
+// caps.  The column-pass variants (two buffers, in place, in place with prefetched
+// weights, two columns per CTA) are timed on the best lengths, and the winner once more
+// with radix-4 rows: a radix-8 row stage of W/8 butterflies per line leaves part of a warp
+// idle when 2W/8 is not a multiple of 32 (W = 576: 144 butterflies on 192 threads), while
+// radix-4 stages fill whole warps.
 struct TunedLayout {
   int H = 0, rc = kMaxRadix, rr = kMaxRadix;
-  bool ip = false, pf = false;
+  bool ip = false, pf = false, ws = false;
   double ms = 0.0;
 };
 std::mutex g_tune_mutex;
@@ -308,8 +322,8 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
   TunedLayout best;
   double best_ms = 1e300;
   const int iters = M >= (1 << 18) ? 10 : 40;
-  auto consider = [&](int H, int rc, int rr, bool ip, bool pf = false) {
-    const double ms = time_layout(M, H, rc, rr, ip, pf, n, sms, iters, s);
+  auto consider = [&](int H, int rc, int rr, bool ip, bool pf = false, bool ws = false) {
+    const double ms = time_layout(M, H, rc, rr, ip, pf, ws, n, sms, iters, s);
     if (ms > 0.0 && ms < best_ms) {
       best_ms = ms;
       best.H = H;
@@ -317,21 +331,30 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
       best.rr = rr;
       best.ip = ip;
       best.pf = pf;
+      best.ws = ws;
     }
   };
   for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
     consider(ranked[i].second, kMaxRadix, kMaxRadix, false);
-    // long columns: the in-place column passes (half the shared memory, 4 CTAs per SM)
+    // the in-place column passes (half the shared memory, 4 CTAs per SM); long columns
+    // also with prefetched weights and two per CTA
+    consider(ranked[i].second, kMaxRadix, kMaxRadix, true);
     if (M >= (1 << 17)) {
-      consider(ranked[i].second, kMaxRadix, kMaxRadix, true);
       consider(ranked[i].second, kMaxRadix, kMaxRadix, true, true);
+      consider(ranked[i].second, kMaxRadix, kMaxRadix, true, false, true);
     }
+  }
+  if (M >= (1 << 17) && best.H) {
+    const TunedLayout b = best;
+    consider(b.H, b.rc, 4, b.ip, b.pf, b.ws);
   }
   if (M < (1 << 17))
     for (size_t i = 0; i < ranked.size() && i < 3; ++i) {
       consider(ranked[i].second, 4, kMaxRadix, false);
       consider(ranked[i].second, kMaxRadix, 4, false);
       consider(ranked[i].second, 4, 4, false);
+      consider(ranked[i].second, 4, 4, true);
+      consider(ranked[i].second, 4, kMaxRadix, true);
       // radix-2 stages: a little more FP64 work per point and bit (3 against 2.75 for
       // radix 4 in ratio form), twice the butterflies per stage, so twice the warps to hide
       // FP64 latency on short lines
@@ -559,7 +582,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     cudaGetLastError();
   }
   if (o.resident > 0 && !resident) return GL_ERR_SIZE;
-  bool col_ip = false, col_pf = false;
+  bool col_ip = false, col_pf = false, col_ws = false;
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
@@ -568,13 +591,16 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
       if (!o.max_radix_row) cap_r = t.rr;
       col_ip = t.ip && !resident;
       col_pf = col_ip && t.pf;
+      col_ws = col_ip && t.ws;
     }
   }
   if (o.col_inplace) {
+    if (o.col_inplace > 3) return GL_ERR_ARG;
     col_ip = o.col_inplace > 0 && !resident && !sms_override;
     col_pf = col_ip && o.col_inplace == 2;
+    col_ws = col_ip && o.col_inplace == 3;
   }
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf)
+  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf, col_ws)
                                    : choose_plain_geom(M, &pg);
   if (rc == GL_ERR_SIZE && col_ip && o.col_inplace <= 0)  // the searched layout cannot: two buffers
     rc = choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, false);
@@ -767,7 +793,7 @@ int gl_plan_get_info(const gl_plan* pl, gl_plan_info* info) {
   info->lo_bits = pl->LO; info->hi_bits = pl->LO + 1;
   info->carry_depth = pl->n; info->mode = pl->mode;
   if (pl->mode == GL_MODE_FUSED) {
-    info->fft_w = pl->fg.W; info->fft_h = pl->fg.H; info->cols_per_cta = pl->fg.G;
+    info->fft_w = pl->fg.W; info->fft_h = pl->fg.H; info->cols_per_cta = pl->fg.col_ws ? 2 : pl->fg.G;
     for (int i = 0; i < pl->fg.pw.nst; ++i) info->radix_w[i] = pl->fg.pw.radix[i];
     for (int i = 0; i < pl->fg.ph.nst; ++i) info->radix_h[i] = pl->fg.ph.radix[i];
     info->threads_col = pl->fg.t_col; info->threads_row = pl->fg.t_row;

@@ -50,6 +50,9 @@ struct FusedGeom {
   int col_ip;                // column passes run their DFTs in place (one buffer, 4 CTAs/SM)
   int col_pf;                // with col_ip: the inverse column pass bulk-copies its weights
                              // and spans into shared memory (18 H bytes more)
+  int col_ws;                // with col_ip: two columns per CTA, one per half of the block
+                             // (2 t_col threads, two in-place line buffers); while one half
+                             // transforms its column the other dices or rounds its own
   int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
                              // a smaller cap means more, shorter butterflies per stage and
                              // so more threads per line, for lengths too short to fill the GPU

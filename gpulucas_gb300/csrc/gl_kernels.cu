@@ -143,6 +143,20 @@ __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, 
   return a;
 }
 
+// The threads that run one line DFT: thread g.tid of g.n, synchronised by barrier g.bar
+// (0: the whole block, __syncthreads; 1, 2: a named barrier of the g.n threads of one half
+// of a block whose two halves work on different columns).
+struct Grp {
+  int tid, n, bar;
+  __device__ __forceinline__ void sync() const {
+    // immediate barrier numbers, so the kernel reserves barriers 0-2 only
+    if (bar == 0) __syncthreads();
+    else if (bar == 1) asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
+    else asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory");
+  }
+};
+__device__ __forceinline__ Grp whole_block() { return Grp{(int)threadIdx.x, (int)blockDim.x, 0}; }
+
 // In-place variant (one buffer, two barriers per stage): every thread first reads the
 // inputs of all its butterflies of the stage into registers (at most 8 points: one radix-8
 // butterfly, two radix-4, four radix-2, one odd-radix), then, after the barrier, computes
@@ -155,14 +169,14 @@ __host__ __device__ constexpr int ip_butterflies() {
 
 template <int R, int S, typename TW>
 __device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nlines, int ls, int L, int Ns,
-                                                  const TW* __restrict__ tw) {
+                                                  const TW* __restrict__ tw, const Grp& g) {
   constexpr int B = ip_butterflies<R>();
   const int LR = L / R;
   const int nb = nlines * LR;
   cplx held[B * R];
 #pragma unroll
   for (int i = 0; i < B; ++i) {
-    const int b = threadIdx.x + i * blockDim.x;
+    const int b = g.tid + i * g.n;
     const int bb = b < nb ? b : 0;  // a thread without this butterfly reads a valid slot
     const int l = bb / LR;
     const int j = bb - l * LR;
@@ -170,10 +184,10 @@ __device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nl
 #pragma unroll
     for (int q = 0; q < R; ++q) held[i * R + q] = s[pad(j + q * LR)];
   }
-  __syncthreads();
+  g.sync();
 #pragma unroll
   for (int i = 0; i < B; ++i) {
-    const int b = threadIdx.x + i * blockDim.x;
+    const int b = g.tid + i * g.n;
     if (b < nb) {
       const int l = b / LR;
       const int j = b - l * LR;
@@ -189,21 +203,22 @@ __device__ __forceinline__ void stockham_stage_ip(cplx* __restrict__ buf, int nl
       for (int q = 0; q < R; ++q) d[pad(base + q * Ns)] = v[q];
     }
   }
-  __syncthreads();
+  g.sync();
 }
 
 template <int S, typename TW>
-__device__ __forceinline__ cplx* line_fft_ip(cplx* a, int nlines, int ls, const LinePlan& lp, const TW* tw) {
+__device__ __forceinline__ cplx* line_fft_ip(cplx* a, int nlines, int ls, const LinePlan& lp, const TW* tw,
+                                             const Grp& g) {
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
     const TW* st = tw + lp.off[s];
     switch (lp.radix[s]) {
-      case 8: stockham_stage_ip<8, S>(a, nlines, ls, lp.L, Ns, st); break;
-      case 4: stockham_stage_ip<4, S>(a, nlines, ls, lp.L, Ns, st); break;
-      case 2: stockham_stage_ip<2, S>(a, nlines, ls, lp.L, Ns, st); break;
-      case 3: stockham_stage_ip<3, S>(a, nlines, ls, lp.L, Ns, st); break;
-      case 5: stockham_stage_ip<5, S>(a, nlines, ls, lp.L, Ns, st); break;
-      default: stockham_stage_ip<7, S>(a, nlines, ls, lp.L, Ns, st); break;
+      case 8: stockham_stage_ip<8, S>(a, nlines, ls, lp.L, Ns, st, g); break;
+      case 4: stockham_stage_ip<4, S>(a, nlines, ls, lp.L, Ns, st, g); break;
+      case 2: stockham_stage_ip<2, S>(a, nlines, ls, lp.L, Ns, st, g); break;
+      case 3: stockham_stage_ip<3, S>(a, nlines, ls, lp.L, Ns, st, g); break;
+      case 5: stockham_stage_ip<5, S>(a, nlines, ls, lp.L, Ns, st, g); break;
+      default: stockham_stage_ip<7, S>(a, nlines, ls, lp.L, Ns, st, g); break;
     }
     Ns *= lp.radix[s];
   }
@@ -238,18 +253,22 @@ __device__ __forceinline__ int colmajor(const IterArgs& a, int j) {
 
 // Column pass, forward.  NC = carry depth n of llintToIrrBal<n>.  For words
 // j0 = 2m, j0+1 the digit sums of j0-1, j0, j0+1 need the products of words
-// j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.
-template <bool FROM_STATE, int NC, bool IP = false>
-__device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
-  extern __shared__ cplx smem[];
-  const int H = a.H, W = a.W, N = a.N;
-  const int ls = a.ls_col;
-  cplx* buf1 = smem + ls;
-  for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
-    const int j0 = 2 * (m1 + W * m2);
+// j0-1-NC .. j0+1: P[k] = product of word j0+1-k, k = 0 .. NC+2.  Words j0+1-2d and
+// j0-2d are the two words of point m-d, column m1-d of the same row (the previous row,
+// from the last columns, when m1 < d), adjacent in the column-major layout: one 16-byte
+// load per point, and no division to find it.
+// Loads column m1 into buf (threads tid, tid + nth, ...): dice the previous products into
+// balanced digits and carries, add the carry of the word below, weight.
+template <bool FROM_STATE, int NC>
+__device__ __forceinline__ void col_fwd_load(const IterArgs& a, const int m1, cplx* buf, int tid, int nth) {
+  const int H = a.H, W = a.W, N = a.N, LO = a.LO;
+  constexpr int D = (NC + 2) / 2;  // points m-1 .. m-D hold the words j0-1 .. j0+1-(NC+2)
+#pragma unroll 1
+  for (int m2 = tid; m2 < H; m2 += nth) {
     const int s0 = 2 * (m1 * H + m2);
     int v0, v1;
     if (FROM_STATE) {
+      const int j0 = 2 * (m1 + W * m2);
       v0 = a.digit[j0] + (int)a.hi[j0 == 0 ? N - 1 : j0 - 1];
       v1 = a.digit[j0 + 1] + (int)a.hi[j0];
     } else {
@@ -257,56 +276,102 @@ __device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
       const longlong2 own = __ldg(reinterpret_cast<const longlong2*>(a.ll + s0));
       P[0] = own.y;
       P[1] = own.x;
+      uint32_t fm = 0;  // flags of word j0-1 (the upper word of point m-1)
 #pragma unroll
-      for (int k = 2; k < NC + 3; ++k) {
-        int j = j0 + 1 - k;
-        if (j < 0) j += N;
-        P[k] = __ldg(a.ll + colmajor(a, j));
+      for (int d = 1; d <= D; ++d) {
+        int c = m1 - d, r = m2;
+        if (c < 0) {  // one wrap suffices: layouts have W >= 4 >= D
+          c += W;
+          r = r == 0 ? H - 1 : r - 1;
+        }
+        const int sd = 2 * (c * H + r);
+        if (d == 1) fm = __ldg(a.flags + sd + 1);
+        if (2 * d + 1 < NC + 3) {
+          const longlong2 v = __ldg(reinterpret_cast<const longlong2*>(a.ll + sd));
+          P[2 * d] = v.y;
+          P[2 * d + 1] = v.x;
+        } else {  // only the upper word of the farthest point
+          P[2 * d] = __ldg(a.ll + sd + 1);
+        }
       }
-      const int jm = j0 == 0 ? N - 1 : j0 - 1;
       const uint32_t f0 = __ldg(a.flags + s0), f1 = __ldg(a.flags + s0 + 1);
-      const uint32_t fm = __ldg(a.flags + colmajor(a, jm));
-      long long sm1 = 0, sw0 = 0, sw1 = 0;
-      {
-        const int LO = a.LO;
-        auto dice_at = [&](uint32_t f, int off) {
-          const long long mask = (1ll << (LO + (int)(f & 1))) - 1;
-          const long long v = P[off];
-          long long sum = v < 0 ? -((-v) & mask) : (v & mask);
-          int shift = 0;
+      auto dice_at = [&](uint32_t f, int off) {
+        const long long mask = (1ll << (LO + (int)(f & 1))) - 1;
+        const long long v = P[off];
+        long long sum = v < 0 ? -((-v) & mask) : (v & mask);
+        int shift = 0;
 #pragma unroll
-          for (int i = 1; i <= NC; ++i) {
-            shift += LO + (int)((f >> i) & 1);
-            const long long w = P[off + i];
-            sum += shift >= 63 ? 0 : (w < 0 ? -(((-w) >> shift) & mask) : ((w >> shift) & mask));
-          }
-          return sum;
-        };
-        sw1 = dice_at(f1, 0);
-        sw0 = dice_at(f0, 1);
-        sm1 = dice_at(fm, 2);
-      }
+        for (int i = 1; i <= NC; ++i) {
+          shift += LO + (int)((f >> i) & 1);
+          const long long w = P[off + i];
+          sum += shift >= 63 ? 0 : (w < 0 ? -(((-w) >> shift) & mask) : ((w >> shift) & mask));
+        }
+        return sum;
+      };
+      const long long sw1 = dice_at(f1, 0), sw0 = dice_at(f0, 1), sm1 = dice_at(fm, 2);
       int dm, hm, d0, h0, d1, h1;
-      balanced_split(sm1, a.LO + (int)(fm & 1), &dm, &hm);
-      balanced_split(sw0, a.LO + (int)(f0 & 1), &d0, &h0);
-      balanced_split(sw1, a.LO + (int)(f1 & 1), &d1, &h1);
+      balanced_split(sm1, LO + (int)(fm & 1), &dm, &hm);
+      balanced_split(sw0, LO + (int)(f0 & 1), &d0, &h0);
+      balanced_split(sw1, LO + (int)(f1 & 1), &d1, &h1);
       v0 = d0 + hm;
       v1 = d1 + h0;
     }
     const double2 A = __ldg(reinterpret_cast<const double2*>(a.A + s0));
-    smem[pad(m2)] = mk(A.x * dbl_from_int(v0), A.y * dbl_from_int(v1));
+    buf[pad(m2)] = mk(A.x * dbl_from_int(v0), A.y * dbl_from_int(v1));
   }
-  __syncthreads();
-  const cplx* res = IP ? line_fft_ip<-1>(smem, 1, ls, a.ph, a.twH) : line_fft<-1>(smem, buf1, 1, ls, a.ph, a.twH);
-  const DevCplx* tw = a.twK1 + (size_t)m1 * H;
-  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x)
-    st(a.Z + (size_t)k2 * W + m1, cmul(res[pad(k2)], ld(tw + k2)));
 }
 
-// IP: the in-place line DFT, half the shared memory, four CTAs per SM
+// twiddle w_M^(m1 k2) and store column m1 into row k2 of Z
+__device__ __forceinline__ void col_fwd_store(const IterArgs& a, const int m1, const cplx* res, int tid, int nth) {
+  const int H = a.H, W = a.W;
+  const DevCplx* tw = a.twK1 + (size_t)m1 * H;
+  for (int k2 = tid; k2 < H; k2 += nth) st(a.Z + (size_t)k2 * W + m1, cmul(res[pad(k2)], ld(tw + k2)));
+}
+
+template <bool FROM_STATE, int NC, bool IP = false>
+__device__ __forceinline__ void col_fwd_body(const IterArgs& a, const int m1) {
+  extern __shared__ cplx smem[];
+  const int ls = a.ls_col;
+  col_fwd_load<FROM_STATE, NC>(a, m1, smem, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const cplx* res = IP ? line_fft_ip<-1>(smem, 1, ls, a.ph, a.twH, whole_block())
+                       : line_fft<-1>(smem, smem + ls, 1, ls, a.ph, a.twH);
+  col_fwd_store(a, m1, res, threadIdx.x, blockDim.x);
+}
+
+// IP: the in-place line DFT, half the shared memory, four CTAs per SM.  The two-buffer
+// form runs where columns are short (a few warps per CTA), so registers do not bound its
+// occupancy: it gets the registers of two 256-thread CTAs per SM.
 template <bool FROM_STATE, int NC, bool IP>
-__global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 3) k_col_fwd(IterArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, IP ? 4 : 2) k_col_fwd(IterArgs a) {
   col_fwd_body<FROM_STATE, NC, IP>(a, blockIdx.x);
+}
+
+// Two columns per CTA, one per half of the block, each half running its column's in-place
+// DFT behind its own named barrier.  A kernel whose CTAs all fit the device at once runs
+// every CTA's phases in step, and the dicing (integer work and loads) leaves the FP64 pipe
+// idle.  Here both halves first dice column c0; then the first half transforms c0 while
+// the second dices c1, and the first half's twiddle-and-store of c0 overlaps the second
+// half's DFT of c1.  The FP64 pipe has work while most of the dicing runs.
+// Each half has kMaxThreads threads (layouts whose columns take kMaxThreads threads).
+template <bool FROM_STATE, int NC>
+__global__ void __launch_bounds__(2 * kMaxThreads, 2) k_col_fwd_ws(IterArgs a) {
+  extern __shared__ cplx smem[];
+  const int ls = a.ls_col;
+  constexpr int half = kMaxThreads;
+  const int c0 = 2 * (int)blockIdx.x, c1 = c0 + 1;
+  const bool second = (int)threadIdx.x >= half;
+  const Grp g{(int)threadIdx.x & (half - 1), half, second ? 2 : 1};
+  col_fwd_load<FROM_STATE, NC>(a, c0, smem, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (second) {
+    if (c1 >= a.W) return;  // odd W: the last CTA has one column (its second half waits on nothing)
+    col_fwd_load<FROM_STATE, NC>(a, c1, smem + ls, g.tid, half);
+    g.sync();
+  }
+  cplx* buf = second ? smem + ls : smem;
+  line_fft_ip<-1>(buf, 1, ls, a.ph, a.twH, g);
+  col_fwd_store(a, second ? c1 : c0, buf, g.tid, half);
 }
 
 // The row pass's stage values (17.4 KB at W = 576) are copied into shared memory behind
@@ -418,44 +483,22 @@ __device__ __forceinline__ long long round_word(double x, int span, unsigned lon
   return r;
 }
 
-// PF (with IP, H a multiple of 8): the column's inverse weights and spans (18 H bytes,
-// contiguous in the column-major tables) are brought into shared memory behind the line
-// buffer by two bulk copies issued at the start, so the rounding loop after the DFT does
-// not wait on global loads.
-template <bool IP = false, bool PF = false>
-__device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
-  static_assert(!PF || IP, "the prefetch area follows the single in-place line buffer");
-  extern __shared__ cplx smem[];
-  __shared__ alignas(8) uint64_t pf_bar;
+// column m1 of the row pass's output (contiguous in Z2) into buf
+__device__ __forceinline__ void col_inv_load(const IterArgs& a, const int m1, cplx* buf, int tid, int nth) {
   const int H = a.H;
-  const int ls = a.ls_col;
-  cplx* buf1 = smem + ls;
-  double* ai_s = reinterpret_cast<double*>(smem + ls);
-  unsigned char* sp_s = reinterpret_cast<unsigned char*>(ai_s + 2 * H);
-  if (PF) {
-    if (threadIdx.x == 0) mbar_init(&pf_bar, 2);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      bulk_load(ai_s, a.Ainv + (size_t)2 * m1 * H, 16u * (uint32_t)H, &pf_bar);
-      bulk_load(sp_s, a.span + (size_t)2 * m1 * H, 2u * (uint32_t)H, &pf_bar);
-    }
-  }
-  for (int k2 = threadIdx.x; k2 < H; k2 += blockDim.x) smem[pad(k2)] = ldc(a.Z2 + (size_t)m1 * H + k2);
-  __syncthreads();
-  const cplx* res = IP ? line_fft_ip<+1>(smem, 1, ls, a.ph, a.twH) : line_fft<+1>(smem, buf1, 1, ls, a.ph, a.twH);
-  if (PF) {
-    const bool ok = mbar_wait(&pf_bar, 0);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) {
-        atomicOr(&a.status->flags, kStatusTimeout);
-        mbar_wait(&pf_bar, 0);  // the copies may still land in this CTA's shared memory
-      }
-      return;
-    }
-  }
+  for (int k2 = tid; k2 < H; k2 += nth) buf[pad(k2)] = ldc(a.Z2 + (size_t)m1 * H + k2);
+}
+
+// Unweight, round, -2 at word 0, range checks and round-off maximum for column m1 from
+// the inverse DFT in res; the inverse weights and spans from shared memory (PF: ai_s,
+// sp_s) or from the column-major tables.
+template <bool PF>
+__device__ __forceinline__ void col_inv_round(const IterArgs& a, const int m1, const cplx* res,
+                                              const double* ai_s, const unsigned char* sp_s, int tid, int nth) {
+  const int H = a.H;
   unsigned long long emax = 0;
   unsigned fl = 0;
-  for (int m2 = threadIdx.x; m2 < H; m2 += blockDim.x) {
+  for (int m2 = tid; m2 < H; m2 += nth) {
     const int s0 = 2 * (m1 * H + m2);
     const cplx v = res[pad(m2)];
     const double2 ai = PF ? make_double2(ai_s[2 * m2], ai_s[2 * m2 + 1])
@@ -470,9 +513,69 @@ __device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
   finish_status(a, emax, fl);
 }
 
+// PF (with IP, H a multiple of 8): the column's inverse weights and spans (18 H bytes,
+// contiguous in the column-major tables) are brought into shared memory behind the line
+// buffer by two bulk copies issued at the start, so the rounding loop after the DFT does
+// not wait on global loads.
+template <bool IP = false, bool PF = false>
+__device__ __forceinline__ void col_inv_body(const IterArgs& a, const int m1) {
+  static_assert(!PF || IP, "the prefetch area follows the single in-place line buffer");
+  extern __shared__ cplx smem[];
+  __shared__ alignas(8) uint64_t pf_bar;
+  const int H = a.H;
+  const int ls = a.ls_col;
+  double* ai_s = reinterpret_cast<double*>(smem + ls);
+  unsigned char* sp_s = reinterpret_cast<unsigned char*>(ai_s + 2 * H);
+  if (PF) {
+    if (threadIdx.x == 0) mbar_init(&pf_bar, 2);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_load(ai_s, a.Ainv + (size_t)2 * m1 * H, 16u * (uint32_t)H, &pf_bar);
+      bulk_load(sp_s, a.span + (size_t)2 * m1 * H, 2u * (uint32_t)H, &pf_bar);
+    }
+  }
+  col_inv_load(a, m1, smem, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const cplx* res = IP ? line_fft_ip<+1>(smem, 1, ls, a.ph, a.twH, whole_block())
+                       : line_fft<+1>(smem, smem + ls, 1, ls, a.ph, a.twH);
+  if (PF) {
+    const bool ok = mbar_wait(&pf_bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&a.status->flags, kStatusTimeout);
+        mbar_wait(&pf_bar, 0);  // the copies may still land in this CTA's shared memory
+      }
+      return;
+    }
+  }
+  col_inv_round<PF>(a, m1, res, ai_s, sp_s, threadIdx.x, blockDim.x);
+}
+
 template <bool IP, bool PF>
 __global__ void __launch_bounds__(kMaxThreads, IP && !PF ? 4 : 3) k_col_inv(IterArgs a) {
   col_inv_body<IP, PF>(a, blockIdx.x);
+}
+
+// Two columns per CTA as in k_col_fwd_ws: both halves load column c0; the first half's
+// inverse DFT of c0 overlaps the second half's load of c1, and the first half's rounding
+// and stores of c0 overlap the second half's DFT of c1.
+__global__ void __launch_bounds__(2 * kMaxThreads, 2) k_col_inv_ws(IterArgs a) {
+  extern __shared__ cplx smem[];
+  const int ls = a.ls_col;
+  constexpr int half = kMaxThreads;
+  const int c0 = 2 * (int)blockIdx.x, c1 = c0 + 1;
+  const bool second = (int)threadIdx.x >= half;
+  const Grp g{(int)threadIdx.x & (half - 1), half, second ? 2 : 1};
+  col_inv_load(a, c0, smem, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (second) {
+    if (c1 >= a.W) return;
+    col_inv_load(a, c1, smem + ls, g.tid, half);
+    g.sync();
+  }
+  cplx* buf = second ? smem + ls : smem;
+  line_fft_ip<+1>(buf, 1, ls, a.ph, a.twH, g);
+  col_inv_round<false>(a, second ? c1 : c0, buf, nullptr, nullptr, g.tid, half);
 }
 
 // ---------------------------------------------------------------------------
@@ -546,12 +649,25 @@ static cudaError_t set_col_fwd_smem(int bytes) {
   return cudaFuncSetAttribute(k_col_fwd<FS, 6, IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+template <bool FS>
+static cudaError_t set_col_fwd_ws_smem(int bytes) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd_ws<FS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd_ws<FS, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd_ws<FS, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_fwd_ws<FS, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+  return cudaFuncSetAttribute(k_col_fwd_ws<FS, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 // The attribute is per kernel and process-wide, shared by every plan: it is raised to the
 // layout chooser's bound once (a launch's occupancy follows its own dynamic size).
 cudaError_t set_fused_smem_limits(const FusedGeom& g) {
   if (g.sm_col > (size_t)kMaxDynSmem || g.sm_cinv > (size_t)kMaxDynSmem || g.sm_row > (size_t)kMaxDynSmem)
     return cudaErrorInvalidValue;
   cudaError_t e;
+  if ((e = set_col_fwd_ws_smem<false>(kMaxDynSmem))) return e;
+  if ((e = set_col_fwd_ws_smem<true>(kMaxDynSmem))) return e;
+  if ((e = cudaFuncSetAttribute(k_col_inv_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<false, false>(kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<true, false>(kMaxDynSmem))) return e;
   if ((e = set_col_fwd_smem<false, true>(kMaxDynSmem))) return e;
@@ -577,13 +693,27 @@ static void launch_col_fwd_ip(const IterArgs& a, const FusedGeom& g, cudaStream_
 }
 
 template <bool FS>
+static void launch_col_fwd_ws(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
+  const int grid = (a.W + 1) / 2, block = 2 * kMaxThreads;
+  switch (a.n) {
+    case 2: k_col_fwd_ws<FS, 2><<<grid, block, g.sm_col, s>>>(a); break;
+    case 3: k_col_fwd_ws<FS, 3><<<grid, block, g.sm_col, s>>>(a); break;
+    case 4: k_col_fwd_ws<FS, 4><<<grid, block, g.sm_col, s>>>(a); break;
+    case 5: k_col_fwd_ws<FS, 5><<<grid, block, g.sm_col, s>>>(a); break;
+    default: k_col_fwd_ws<FS, 6><<<grid, block, g.sm_col, s>>>(a); break;
+  }
+}
+
+template <bool FS>
 static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  if (g.col_ip) launch_col_fwd_ip<FS, true>(a, g, s);
+  if (g.col_ws) launch_col_fwd_ws<FS>(a, g, s);
+  else if (g.col_ip) launch_col_fwd_ip<FS, true>(a, g, s);
   else launch_col_fwd_ip<FS, false>(a, g, s);
 }
 
 static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
+  if (g.col_ws) k_col_inv_ws<<<(a.W + 1) / 2, 2 * kMaxThreads, g.sm_cinv, s>>>(a);
+  else if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
   else if (g.col_ip) k_col_inv<true, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
   else k_col_inv<false, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
 }

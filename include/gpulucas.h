@@ -66,7 +66,9 @@ typedef struct {
                               1 = require (N <= 32768), -1 = never */
     int col_inplace;       /* fused form: column passes with in-place line DFTs (one buffer,
                               four CTAs per SM); 2: also bulk-copy the inverse pass's weights
-                              into shared memory; 0 = the autotuner decides, -1 = never */
+                              into shared memory; 3: two columns per CTA, one per half of the
+                              block, so that one half's dicing or rounding overlaps the other
+                              half's DFT; 0 = the autotuner decides, -1 = never */
     int reserved[1];
 } gl_plan_opts;
 
@@ -76,7 +78,7 @@ typedef struct {
     int carry_depth;       /* n of llintToIrrBal<n> (setSliceAndDice, gpuLucas.cu:323-343) */
     int mode;
     int fft_w, fft_h;      /* N/2 = fft_w * fft_h complex points */
-    int cols_per_cta;
+    int cols_per_cta;      /* columns per CTA of the column passes (1, or 2 with col_inplace 3) */
     int radix_w[8], radix_h[8];
     int threads_col, threads_row;  /* CTA sizes of the column and row passes */
     int smem_col, smem_row;        /* dynamic shared memory bytes of those passes */

@@ -132,6 +132,39 @@ def test_inplace_column_passes_match(gl, orc, p, N, H, mode):
             assert (pa == o.ll()).all()
 
 
+@pytest.mark.parametrize("p,N", [(2000003, 131072), (645131, 36864), (43112609, 2359296)],
+                         ids=["depth4-W64", "depth3-W9-odd", "C3"])
+def test_two_column_passes_match_oracle(gl, orc, p, N):
+    """Two columns per CTA (col_inplace 3: each half of the block runs one column's in-place
+    DFT behind its own named barrier, so one half's dicing or rounding overlaps the other
+    half's DFT) gives the products of the two-buffer form and of the oracle: carry depths 4
+    and 3 (ratio 15 and 17), an odd number of columns (the last CTA holds one), C3; and
+    after a resume from a carry-save state, where the first forward pass loads digits and
+    carries instead of dicing products."""
+    H = 2048
+    with gl.Plan(p, N, col_inplace=3, fft_h=H, autotune=0) as a, \
+            gl.Plan(p, N, col_inplace=-1, fft_h=H, autotune=0) as b:
+        assert a.info.cols_per_cta == 2 and b.info.cols_per_cta == 1
+        assert a.info.fft_h == H and a.info.threads_col == 256
+        o = orc.IBDWT(p, N) if N <= 163840 else None
+        done = 0
+        for k in (1, 6):
+            a.iterate(k)
+            b.iterate(k)
+            done += k
+            pa = a.products()
+            assert (pa == b.products()).all(), f"iteration {done}"
+            if o is not None:
+                o.iterate(k)
+                assert (pa == o.ll()).all(), f"iteration {done}"
+        d, h = b.carry_state()
+        b.iterate(5)
+        a.set_carry_state(d, h, done)
+        a.iterate(5)
+        assert (a.products() == b.products()).all()
+        assert a.res64() == b.res64()
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432), (2976221, 163840)])
 @pytest.mark.parametrize("caps", [(4, 4), (2, 2), (4, 8), (8, 2)])
 def test_radix_capped_layouts_match_oracle(gl, orc, p, N, caps):
