@@ -154,6 +154,7 @@ def _load():
         "gl_set_products": (ctypes.c_int, [P, vp, ctypes.c_int64]),
         "gl_set_carry_state": (ctypes.c_int, [P, vp, vp, ctypes.c_int64]),
         "gl_iterate_host": (ctypes.c_int, [P, vp, vp, ctypes.c_int64, vp, vp, ctypes.POINTER(IterReport)]),
+        "gl_iterate_host_words": (ctypes.c_int, [P, vp, ctypes.c_int64, vp, ctypes.POINTER(IterReport)]),
         "gl_get_residue": (ctypes.c_int, [P, vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
         "errorTest": (ctypes.c_float, [ctypes.c_int, ctypes.c_int]),
         "mersenneTest": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
@@ -224,7 +225,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query", "gl_fast_signal_size",
     "gl_server_default_opts", "gl_server_create", "gl_server_submit", "gl_server_poll", "gl_server_drain",
     "gl_server_checkpoints", "gl_server_get_stats", "gl_server_destroy", "gl_selftest_bounded_wait",
-    "gl_iterate_host",
+    "gl_iterate_host", "gl_iterate_host_words",
 ]))
 
 
@@ -353,6 +354,17 @@ class Plan:
         if check:
             _check(st, "iterate_host")
         return do, ho, rep
+
+    def iterate_host_words(self, words: np.ndarray, iters: int, check: bool = True):
+        """(words, report): `iters` iterations from host-held carry-added words
+        (digit[j] + hi[j-1], 4 bytes per word)."""
+        w = np.ascontiguousarray(words, np.int32)
+        out = np.empty(self.N, np.int32)
+        rep = IterReport()
+        st = lib.gl_iterate_host_words(self._h, _ptr(w), int(iters), _ptr(out), ctypes.byref(rep))
+        if check:
+            _check(st, "iterate_host_words")
+        return out, rep
 
     def set_carry_state(self, digit: np.ndarray, hi: np.ndarray, iterations: int):
         d = np.ascontiguousarray(digit, np.int32)

@@ -210,17 +210,17 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
     g->col_ip = 1;
     g->sm_col = g->sm_cinv = (size_t)g->ls_col * 16;
     if (ws) {
-      // two columns per CTA: two in-place line buffers, no prefetch area
+      // two columns per CTA: two in-place line buffers; the inverse pass too, unless it
+      // prefetches its weights (then it keeps one column per CTA)
       if (g->W < 2 || g->t_col != kMaxThreads) return GL_ERR_SIZE;
       g->col_ws = 1;
       g->sm_col = g->sm_cinv = (size_t)2 * g->ls_col * 16;
       if (g->sm_col > (size_t)kMaxDynSmem) return GL_ERR_SIZE;
-      return GL_OK;
     }
     if (pf) {
       if (g->H % 8) return GL_ERR_SIZE;  // bulk copies of 2H bytes must be 16-byte multiples
       g->col_pf = 1;
-      g->sm_cinv += (size_t)18 * g->H;
+      g->sm_cinv = (size_t)g->ls_col * 16 + (size_t)18 * g->H;
     }
   }
   return GL_OK;
@@ -342,6 +342,7 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
     if (M >= (1 << 17)) {
       consider(ranked[i].second, kMaxRadix, kMaxRadix, true, true);
       consider(ranked[i].second, kMaxRadix, kMaxRadix, true, false, true);
+      consider(ranked[i].second, kMaxRadix, kMaxRadix, true, true, true);
     }
   }
   if (M >= (1 << 17) && best.H) {
@@ -595,10 +596,10 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     }
   }
   if (o.col_inplace) {
-    if (o.col_inplace > 3) return GL_ERR_ARG;
+    if (o.col_inplace > 4) return GL_ERR_ARG;
     col_ip = o.col_inplace > 0 && !resident && !sms_override;
-    col_pf = col_ip && o.col_inplace == 2;
-    col_ws = col_ip && o.col_inplace == 3;
+    col_pf = col_ip && (o.col_inplace == 2 || o.col_inplace == 4);
+    col_ws = col_ip && (o.col_inplace == 3 || o.col_inplace == 4);
   }
   int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf, col_ws)
                                    : choose_plain_geom(M, &pg);
@@ -985,6 +986,48 @@ int gl_iterate_host(gl_plan* pl, const int32_t* digit_in, const int8_t* hi_in, i
   if (rc != GL_OK) return rc;
   GL_CUDA(cudaMemcpyAsync(digit_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaMemcpyAsync(hi_out, pl->args.hi, N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
+  GL_CUDA(cudaEventSynchronize(pl->ev1));
+  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
+  if (e > pl->run_maxerr) pl->run_maxerr = e;
+  int st = GL_OK;
+  if (pl->h_status->flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
+  else if (pl->h_status->flags) st = GL_ERR_OVERFLOW;
+  else if (e >= pl->error_limit) st = GL_ERR_ROUNDOFF;
+  float ms = 0.f;
+  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
+  if (rep) {
+    rep->iterations = iters;
+    rep->total_iterations = pl->iters_done;
+    rep->max_roundoff = e;
+    rep->ms = ms;
+    rep->status = st;
+  }
+  return st;
+}
+
+int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, int32_t* words_out,
+                          gl_iter_report* rep) {
+  if (!pl || !words_in || !words_out || iters < 0) return GL_ERR_ARG;
+  GL_CUDA(cudaSetDevice(pl->device));
+  const size_t N = (size_t)pl->N;
+  GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->args.digit, words_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.hi, 0, N, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream));
+  pl->from_state = pl->mode == GL_MODE_FUSED;
+  pl->carry_valid = true;
+  if (iters > 0) {
+    const int rc = enqueue(pl, iters);
+    if (rc != GL_OK) return rc;
+    pl->iters_done += iters;
+    pl->carry_valid = pl->mode == GL_MODE_PLAIN;
+  }
+  const int rc = ensure_carry(pl);
+  if (rc != GL_OK) return rc;
+  GL_CUDA(launch_add_carry(pl->args, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(words_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
   GL_CUDA(cudaEventSynchronize(pl->ev1));

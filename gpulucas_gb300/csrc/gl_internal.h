@@ -52,7 +52,8 @@ struct FusedGeom {
                              // and spans into shared memory (18 H bytes more)
   int col_ws;                // with col_ip: two columns per CTA, one per half of the block
                              // (2 t_col threads, two in-place line buffers); while one half
-                             // transforms its column the other dices or rounds its own
+                             // transforms its column the other dices or rounds its own (the
+                             // inverse pass keeps one column per CTA when col_pf is set)
   int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
                              // a smaller cap means more, shorter butterflies per stage and
                              // so more threads per line, for lengths too short to fill the GPU
@@ -141,6 +142,8 @@ cudaError_t launch_set_initial(const IterArgs& a, int mode, cudaStream_t s);
 cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
 // fused form: dice the column-major products into natural-order (digit, hi)
 cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
+// (digit, hi) -> (digit + hi[j-1], 0): the carry-added words, the same state
+cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s);
 // fused form: natural <-> column-major copies of an int64 word array
 cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
                                  cudaStream_t s);

@@ -712,8 +712,8 @@ static void launch_col_fwd(const IterArgs& a, const FusedGeom& g, cudaStream_t s
 }
 
 static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
-  if (g.col_ws) k_col_inv_ws<<<(a.W + 1) / 2, 2 * kMaxThreads, g.sm_cinv, s>>>(a);
-  else if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
+  if (g.col_ip && g.col_pf) k_col_inv<true, true><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
+  else if (g.col_ws) k_col_inv_ws<<<(a.W + 1) / 2, 2 * kMaxThreads, g.sm_cinv, s>>>(a);
   else if (g.col_ip) k_col_inv<true, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
   else k_col_inv<false, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
 }
@@ -763,6 +763,21 @@ __global__ void k_dice_perm(IterArgs a) {
   balanced_split(s, a.LO + (int)(f & 1), &d, &h);
   a.digit[j] = d;
   a.hi[j] = (signed char)h;
+}
+
+// digit[j] += hi[j-1 mod N] (addPseudoBalanced, IrrBaseBalanced.cu:117-125); the caller
+// clears hi afterwards, so (digit, 0) is the same carry-save state
+__global__ void k_add_carry(IterArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.N) return;
+  a.digit[j] += (int)a.hi[j == 0 ? a.N - 1 : j - 1];
+}
+
+cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s) {
+  k_add_carry<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaMemsetAsync(a.hi, 0, (size_t)a.N, s);
 }
 
 cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s) {

@@ -68,7 +68,8 @@ typedef struct {
                               four CTAs per SM); 2: also bulk-copy the inverse pass's weights
                               into shared memory; 3: two columns per CTA, one per half of the
                               block, so that one half's dicing or rounding overlaps the other
-                              half's DFT; 0 = the autotuner decides, -1 = never */
+                              half's DFT; 4: 3 for the forward pass, 2 for the inverse pass;
+                              0 = the autotuner decides, -1 = never */
     int reserved[1];
 } gl_plan_opts;
 
@@ -78,7 +79,8 @@ typedef struct {
     int carry_depth;       /* n of llintToIrrBal<n> (setSliceAndDice, gpuLucas.cu:323-343) */
     int mode;
     int fft_w, fft_h;      /* N/2 = fft_w * fft_h complex points */
-    int cols_per_cta;      /* columns per CTA of the column passes (1, or 2 with col_inplace 3) */
+    int cols_per_cta;      /* columns per CTA of the forward column pass (1, or 2 with
+                              col_inplace 3 or 4) */
     int radix_w[8], radix_h[8];
     int threads_col, threads_row;  /* CTA sizes of the column and row passes */
     int smem_col, smem_row;        /* dynamic shared memory bytes of those passes */
@@ -159,6 +161,15 @@ int gl_set_products(gl_plan* plan, const int64_t* ll, int64_t iterations);
  * buffers copy at the CPU link's full rate. */
 int gl_iterate_host(gl_plan* plan, const int32_t* digit_in, const int8_t* hi_in, int64_t iters,
                     int32_t* digit_out, int8_t* hi_out, gl_iter_report* report);
+/* The same with the state as carry-added words, 4 bytes per word instead of 5: word j is
+ * digit[j] + hi[j-1] (mod N), the integer that loadIntToDoubleIBDWT weights into the
+ * next FFT input (gpuLucas.cu:730-766) and that addPseudoBalanced forms
+ * (IrrBaseBalanced.cu:117-125).  Loading words w continues exactly as the carry-save
+ * state it came from (the next FFT input is the same), and the words returned are the
+ * carry-save state after the iterations with its carries added.  words_in may alias
+ * words_out. */
+int gl_iterate_host_words(gl_plan* plan, const int32_t* words_in, int64_t iters, int32_t* words_out,
+                          gl_iter_report* report);
 /* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */
 int gl_set_carry_state(gl_plan* plan, const int32_t* digit, const int8_t* hi, int64_t iterations);
 

@@ -134,15 +134,17 @@ def test_inplace_column_passes_match(gl, orc, p, N, H, mode):
 
 @pytest.mark.parametrize("p,N", [(2000003, 131072), (645131, 36864), (43112609, 2359296)],
                          ids=["depth4-W64", "depth3-W9-odd", "C3"])
-def test_two_column_passes_match_oracle(gl, orc, p, N):
+@pytest.mark.parametrize("variant", [3, 4], ids=["both-two-column", "fwd-two-column+inv-prefetch"])
+def test_two_column_passes_match_oracle(gl, orc, p, N, variant):
     """Two columns per CTA (col_inplace 3: each half of the block runs one column's in-place
     DFT behind its own named barrier, so one half's dicing or rounding overlaps the other
     half's DFT) gives the products of the two-buffer form and of the oracle: carry depths 4
     and 3 (ratio 15 and 17), an odd number of columns (the last CTA holds one), C3; and
     after a resume from a carry-save state, where the first forward pass loads digits and
-    carries instead of dicing products."""
+    carries instead of dicing products.  Variant 4 pairs the two-column forward pass with the
+    single-column inverse pass that prefetches its weights."""
     H = 2048
-    with gl.Plan(p, N, col_inplace=3, fft_h=H, autotune=0) as a, \
+    with gl.Plan(p, N, col_inplace=variant, fft_h=H, autotune=0) as a, \
             gl.Plan(p, N, col_inplace=-1, fft_h=H, autotune=0) as b:
         assert a.info.cols_per_cta == 2 and b.info.cols_per_cta == 1
         assert a.info.fft_h == H and a.info.threads_col == 256
@@ -256,6 +258,38 @@ def test_iterate_host_state_chain(gl, orc, p, N, mode):
             assert rep.status == 0 and (d == d2).all() and (h == h2).all()
         pl.set_carry_state(d, h, 15)
         assert pl.res64() == orc.Exact(p).iterate(15).res64()
+
+
+@pytest.mark.parametrize("p,N,mode", [(44497, 2048, 0), (1000003, 54432, 0), (100003, 5184, 1),
+                                      (43112609, 2359296, 0)])
+def test_iterate_host_words_chain(gl, orc, p, N, mode):
+    """gl_iterate_host_words (the state as carry-added words, digit[j] + hi[j-1]) follows the
+    carry-save chain exactly: after each call the words equal the oracle's state with its
+    carries added, and the products equal the oracle's (the continuation from (words, 0)
+    feeds the same FFT input as (digit, hi)).  C3 is checked against the carry-save path."""
+    if N > 200000:
+        with gl.Plan(p, N) as a, gl.Plan(p, N) as b:
+            d = np.zeros(N, np.int32)
+            d[0] = 4                      # S0 = 4
+            h = np.zeros(N, np.int8)
+            w = d.copy()
+            for k in (1, 4):
+                w, rep = a.iterate_host_words(w, k)
+                d, h, _ = b.iterate_host(d, h, k)
+                assert rep.status == 0 and (w == d + np.roll(h.astype(np.int32), 1)).all()
+            assert (a.products() == b.products()).all()
+        return
+    o = orc.IBDWT(p, N)
+    d, h = o.state()
+    w = d + np.roll(h.astype(np.int32), 1)
+    with gl.Plan(p, N, mode=mode) as pl:
+        for k in (1, 3, 10):
+            w, rep = pl.iterate_host_words(w, k)
+            o.iterate(k)
+            d2, h2 = o.state()
+            assert rep.status == 0 and (w == d2 + np.roll(h2.astype(np.int32), 1)).all()
+            assert (pl.products() == o.ll()).all()
+        assert pl.res64() == orc.Exact(p).iterate(14).res64()
 
 
 @pytest.mark.parametrize("p,N,mode", [(1000003, 54432, 0), (100003, 5184, 1), (44497, 2048, 0)])
