@@ -336,6 +336,9 @@ def run_ours(args, world: int, rank: int, local: int):
         "data": "synthetic: the LL sequence from S0=4 (no dataset)",
         "config": {"workload": WORKLOAD,
                    "p": P3, "N": N3, "fft": f"{info.fft_h} x {info.fft_w}", "parallelism": "replicas",
+                   "layout": {"radix_h": [r for r in info.radix_h if r], "radix_w": [r for r in info.radix_w if r],
+                              "column_variant": info.col_variant, "threads_col": info.threads_col,
+                              "threads_row": info.threads_row},
                    "l2": "flushed before every timed step (512 MiB write); the test's ~170 MB of state and "
                          "tables exceed the 129 MB L2 anyway",
                    "vs_baseline_note": "reference's published 204.72 iter/s at N=2359296 (GTX 480/C2050)"},

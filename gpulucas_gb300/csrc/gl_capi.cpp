@@ -795,6 +795,7 @@ int gl_plan_get_info(const gl_plan* pl, gl_plan_info* info) {
   info->carry_depth = pl->n; info->mode = pl->mode;
   if (pl->mode == GL_MODE_FUSED) {
     info->fft_w = pl->fg.W; info->fft_h = pl->fg.H; info->cols_per_cta = pl->fg.col_ws ? 2 : pl->fg.G;
+    info->col_variant = !pl->fg.col_ip ? -1 : pl->fg.col_ws ? (pl->fg.col_pf ? 4 : 3) : (pl->fg.col_pf ? 2 : 1);
     for (int i = 0; i < pl->fg.pw.nst; ++i) info->radix_w[i] = pl->fg.pw.radix[i];
     for (int i = 0; i < pl->fg.ph.nst; ++i) info->radix_h[i] = pl->fg.ph.radix[i];
     info->threads_col = pl->fg.t_col; info->threads_row = pl->fg.t_row;

@@ -29,7 +29,7 @@ void on_signal(int) { g_stop = 1; }
 void usage() {
   std::fprintf(stderr,
                "usage: gpulucas [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] "
-               "[-H h] [-I mode] [p]\n"
+               "[-H h] [-I mode] [-R radix] [p]\n"
                "  -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); default: timed search\n"
                "  -n p    exponent of 2^p - 1 (or give it as the last argument)\n"
                "  -d dev  CUDA device\n"
@@ -37,7 +37,9 @@ void usage() {
                "  -k k    stop after k iterations and print Res64 (default: full p-2 test)\n"
                "  -m      fused (default) or plain execution form\n"
                "  -H h    fused layout column length\n"
-               "  -I mode column passes: 1 in place, 2 in place + prefetch, -1 two buffers\n"
+               "  -I mode column passes: 1 in place, 2 in place + prefetch, 3 two columns per CTA,\n"
+               "          4 two columns per CTA forward + prefetch inverse, -1 two buffers\n"
+               "  -R r    largest radix of the row DFTs (8, 4 or 2)\n"
                "  -v -q   verbose / quiet\n");
 }
 
@@ -56,7 +58,7 @@ int fail(const char* what, int st) {
 
 int main(int argc, char** argv) {
   bool verbose = false, quiet = false;
-  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED, inplace = 0;
+  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED, inplace = 0, row_radix = 0;
   long long freq = 0, k = 0;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
@@ -79,6 +81,7 @@ int main(int argc, char** argv) {
     else if (a == "-k") k = std::atoll(next("-k"));
     else if (a == "-H") fft_h = std::atoi(next("-H"));
     else if (a == "-I") inplace = std::atoi(next("-I"));
+    else if (a == "-R") row_radix = std::atoi(next("-R"));
     else if (a == "-m") {
       const std::string m = next("-m");
       if (m == "fused") mode = GL_MODE_FUSED;
@@ -120,6 +123,7 @@ int main(int argc, char** argv) {
   o.mode = mode;
   o.fft_h = fft_h;
   o.col_inplace = inplace;
+  o.max_radix_row = row_radix;
   if (!N) {
     double ms = 0.0, err = 0.0;
     const int st = gl_find_signal_size(p, &o, &N, &ms, &err);

@@ -87,6 +87,9 @@ typedef struct {
     size_t device_bytes;   /* device memory held by the plan */
     int resident_ctas;     /* CTAs of the resident form's cluster, 0 if not used */
     int resident_smem;     /* its shared memory per CTA */
+    int col_variant;       /* fused form: the column passes as a col_inplace value (-1 two
+                              buffers, 1 in place, 2 + prefetched weights, 3 two columns per
+                              CTA, 4 two columns forward + prefetched weights inverse) */
 } gl_plan_info;
 
 typedef struct {
