@@ -252,6 +252,7 @@ def run_ours(args, world: int, rank: int, local: int):
     dev = local
     torch.cuda.set_device(dev)
     peak = gl.probe_fp64_peak(dev, 400.0)
+    bfly = gl.probe_fp64_butterfly(dev, 400.0)
     plan = gl.Plan(P3, N3, device=dev, check_every=1 << 30)
     info = plan.info
     stream = torch.cuda.ExternalStream(plan.stream)
@@ -347,6 +348,10 @@ def run_ours(args, world: int, rank: int, local: int):
                      "peak_source": "measured live: DFMA probe (gl_probe_fp64_peak); MEASURED_PEAKS.json has "
                                     "no FP64 figure",
                      "algorithmic_flops_per_launch": kf[dom], "kernel_ms": prof,
+                     "butterfly_issue": {"fp64_instr_per_s": bfly, "of_dfma_probe": bfly / (peak * 0.5e12),
+                                         "note": "FP64 issue rate of the line DFTs' twiddled radix-8 butterfly "
+                                                 "from registers (gl_probe_fp64_butterfly), beside the DFMA "
+                                                 "probe's rate (peak/2 instructions per second)"},
                      "iteration_flop_alg": flop_alg(N3),
                      "iteration_tflops": flop_alg(N3) / (iter_ms * 1e-3) / 1e12,
                      "hbm_gbs_alg": 16.0 * N3 / (iter_ms * 1e-3) / 1e9},

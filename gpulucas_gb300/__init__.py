@@ -165,6 +165,7 @@ def _load():
         "gl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
         "gl_version": (ctypes.c_int, []),
         "gl_probe_fp64_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+        "gl_probe_fp64_butterfly": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         "gl_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
         "gl_find_signal_size": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(PlanOpts), ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
@@ -219,7 +220,7 @@ ABI_SYMBOLS = tuple(sorted([
     "gl_get_products",
     "gl_get_carry_state", "gl_set_products", "gl_set_carry_state", "gl_get_residue", "errorTest",
     "mersenneTest", "setSliceAndDice", "gl_error_test", "gl_mersenne_test", "gl_error_string", "gl_version",
-    "gl_probe_fp64_peak", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
+    "gl_probe_fp64_peak", "gl_probe_fp64_butterfly", "gl_iterate_noalloc", "gl_find_signal_size", "gl_checkpoint_write",
     "gl_checkpoint_read", "gl_plan_resume", "gl_smallest_signal_size", "gl_batch_create", "gl_batch_destroy",
     "gl_batch_iterate", "gl_batch_stream", "gl_batch_enqueue", "gl_batch_sync_status", "gl_batch_result",
     "gl_batch_get_info", "gl_batch_test_info", "gl_batch_create_from_plans", "gl_batch_test_status", "gl_safe_signal_size", "gl_batch_query", "gl_fast_signal_size",
@@ -581,6 +582,13 @@ def iterate_noalloc(p: int, N: int, ll_in_ptr: int, ll_out_ptr: int, iters: int,
 def probe_fp64_peak(device: int = 0, ms: float = 200.0) -> float:
     t = ctypes.c_double()
     _check(lib.gl_probe_fp64_peak(int(device), float(ms), ctypes.byref(t)), "probe_fp64_peak")
+    return t.value
+
+
+def probe_fp64_butterfly(device: int = 0, ms: float = 200.0) -> float:
+    """FP64 instructions per second of the line DFTs' radix-8 butterfly (registers only)."""
+    t = ctypes.c_double()
+    _check(lib.gl_probe_fp64_butterfly(int(device), float(ms), ctypes.byref(t)), "probe_fp64_butterfly")
     return t.value
 
 

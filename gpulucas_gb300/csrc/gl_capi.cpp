@@ -1259,8 +1259,11 @@ int gl_selftest_bounded_wait(int device, int tries) {
   return (h.flags & kStatusTimeout) ? GL_ERR_TIMEOUT : GL_OK;
 }
 
-int gl_probe_fp64_peak(int device, double ms, double* tflops) {
-  if (!tflops || ms <= 0) return GL_ERR_ARG;
+// Runs probe(blocks, threads, iters) with iters doubling until one launch takes >= ms;
+// returns its milliseconds and the iteration count.
+}  // extern "C"
+template <typename Probe>
+static int timed_probe(int device, double ms, Probe probe, float* el_out, long long* iters_out, int* blocks_out) {
   GL_CUDA(cudaSetDevice(device));
   int nsm = 0;
   GL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
@@ -1275,20 +1278,43 @@ int gl_probe_fp64_peak(int device, double ms, double* tflops) {
   int rc = GL_OK;
   for (int rep = 0; rep < 12; ++rep) {
     cudaEventRecord(a, 0);
-    if (probe_fp64(blocks, threads, iters, buf, 0) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
+    if (probe(blocks, threads, iters, buf, (cudaStream_t)0) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
     cudaEventRecord(b, 0);
     if (cudaEventSynchronize(b) != cudaSuccess) { rc = GL_ERR_CUDA; break; }
     cudaEventElapsedTime(&el, a, b);
     if (el >= ms) break;
     iters *= 2;
   }
-  if (rc == GL_OK) {
-    const double fmas = (double)blocks * threads * 8.0 * (double)iters;
-    *tflops = 2.0 * fmas / (el * 1e-3) / 1e12;
-  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(buf);
+  *el_out = el;
+  *iters_out = iters;
+  *blocks_out = blocks;
+  return rc;
+}
+extern "C" {
+
+int gl_probe_fp64_peak(int device, double ms, double* tflops) {
+  if (!tflops || ms <= 0) return GL_ERR_ARG;
+  float el = 0.f;
+  long long iters = 0;
+  int blocks = 0;
+  const int rc = timed_probe(device, ms, probe_fp64, &el, &iters, &blocks);
+  if (rc == GL_OK) {
+    const double fmas = (double)blocks * 256 * 8.0 * (double)iters;
+    *tflops = 2.0 * fmas / (el * 1e-3) / 1e12;
+  }
+  return rc;
+}
+
+int gl_probe_fp64_butterfly(int device, double ms, double* instr_per_s) {
+  if (!instr_per_s || ms <= 0) return GL_ERR_ARG;
+  float el = 0.f;
+  long long iters = 0;
+  int blocks = 0;
+  const int rc = timed_probe(device, ms, probe_butterfly, &el, &iters, &blocks);
+  if (rc == GL_OK) *instr_per_s = (double)blocks * 256 * kProbeButterflyInstr * (double)iters / (el * 1e-3);
   return rc;
 }
 

@@ -161,5 +161,8 @@ size_t residue_head_offset(int N);
 cudaError_t launch_residue(const IterArgs& a, bool colmajor_flags, int32_t* balanced, void* scratch,
                            cudaStream_t s);
 cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cudaStream_t s);
+// 82 FP64 instructions per round and thread (the twiddled radix-8 butterfly and a rescale)
+constexpr int kProbeButterflyInstr = 82;
+cudaError_t probe_butterfly(int blocks, int threads, long long iters, double* out, cudaStream_t s);
 
 }  // namespace gl

@@ -946,6 +946,38 @@ cudaError_t probe_fp64(int blocks, int threads, long long iters, double* out, cu
   return cudaGetLastError();
 }
 
+// FP64 issue-rate probe on butterfly code: each thread applies the twiddled radix-8 stage
+// butterfly of the line DFTs (ratio form, stored values read from shared memory) to eight
+// points held in registers, then scales them by 1/8 to keep them bounded, `iters` times.
+// 66 + 16 FP64 instructions per round (62 DFMA + 4 DADD in the butterfly, 16 DMUL).
+__global__ void k_probe_butterfly(double* out, long long iters) {
+  __shared__ cplx tab[32];
+  if (threadIdx.x < 32) {
+    const double t = 0.01 * (threadIdx.x & 7);
+    tab[threadIdx.x] = mk(0.3 + t, 0.9 - t);
+    if ((threadIdx.x & 7) == 1) tab[threadIdx.x].im = bits_dbl(0);  // flags word: no i^f rotations
+  }
+  __syncthreads();
+  cplx v[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[q] = mk(threadIdx.x * 1e-3 + q, q * 0.5);
+  const int base = (threadIdx.x & 3) * 8;
+  for (long long i = 0; i < iters; ++i) {
+    stage_dft<8, -1>(v, true, [&](int k) { return tab[base + k]; });
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = mk(v[q].re * 0.125, v[q].im * 0.125);
+  }
+  double acc = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc += v[q].re + v[q].im;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+cudaError_t probe_butterfly(int blocks, int threads, long long iters, double* out, cudaStream_t s) {
+  k_probe_butterfly<<<blocks, threads, 0, s>>>(out, iters);
+  return cudaGetLastError();
+}
+
 
 // ---------------------------------------------------------------------------
 // Resident form: one cluster holds the test (see ResidentGeom in gl_internal.h).  Per

@@ -396,6 +396,12 @@ int gl_selftest_bounded_wait(int device, int tries);
 /* FP64 throughput probe (DFMA), for the roofline denominator: TFLOP/s counting an FMA
  * as 2 flops, measured on `device` for about `ms` milliseconds. */
 int gl_probe_fp64_peak(int device, double ms, double* tflops);
+/* FP64 issue rate of butterfly code: the twiddled radix-8 butterfly of the line DFTs
+ * applied to register-resident points on all SMs for about `ms` milliseconds; FP64
+ * instructions per second (one per DFMA, DADD or DMUL).  Compiled FP64 code with data
+ * dependences issues below the DFMA probe's rate; this is the rate the FFT's own
+ * instruction mix reaches when nothing else (shared memory, barriers) intervenes. */
+int gl_probe_fp64_butterfly(int device, double ms, double* instr_per_s);
 
 #ifdef __cplusplus
 }

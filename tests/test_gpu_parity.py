@@ -341,3 +341,13 @@ def test_find_signal_size(gl, orc):
         assert pl.info.N == N
         pl.iterate(300)
         assert pl.res64() == orc.Exact(p).iterate(300).res64()
+
+
+def test_fp64_probes(gl):
+    """The DFMA peak probe (the roofline denominator) and the butterfly issue-rate probe
+    run and report plausible rates: the butterfly code issues FP64 instructions no faster
+    than independent DFMA chains do."""
+    peak = gl.probe_fp64_peak(0, 50.0)
+    bfly = gl.probe_fp64_butterfly(0, 50.0)
+    assert 0.3 < peak < 5.0                       # TFLOP/s
+    assert 0.2 * peak * 0.5e12 < bfly < 1.05 * peak * 0.5e12
