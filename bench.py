@@ -441,7 +441,10 @@ def batched_leg(gl, dev: int, iters: int) -> dict:
     t0 = time.perf_counter()
     b = gl.Batch(ps, Ns, device=dev, check_every=1000)
     build_s = time.perf_counter() - t0
+    import torch
+    torch.cuda.nvtx.range_push("batched_steps")  # lets a profiler select the batch's launches
     rep = b.iterate(iters, check=False)
+    torch.cuda.nvtx.range_pop()
     status = [b.test_status(i) for i in range(len(ps))]
     info = b.info
     b.close()
@@ -452,6 +455,15 @@ def batched_leg(gl, dev: int, iters: int) -> dict:
     fused = serve.measure_ms_per_iter(pairs, gl.MODE_FUSED, device=dev, iters=200)
     seq_plain = sum(plain[N] for N in Ns) * iters * 1e-3
     seq_fused = sum(fused[N] for N in Ns) * iters * 1e-3
+    # measured check of the model: 16 members spread over the length range, run one at a
+    # time for the batch's iterations in each form
+    order = sorted(range(len(ps)), key=lambda i: Ns[i])
+    sub = [order[i * (len(order) - 1) // 15] for i in range(16)]
+    check = {}
+    for name, mode, ms in (("plain", gl.MODE_PLAIN, plain), ("fused", gl.MODE_FUSED, fused)):
+        meas = sum(serve.run_sequential([(ps[i], Ns[i], iters) for i in sub], mode, device=dev))
+        model = sum(ms[Ns[i]] for i in sub) * iters * 1e-3
+        check[name] = {"tests": len(sub), "model_s": model, "measured_s": meas, "measured_over_model": meas / model}
     return {
         "workload": f"{len(ps)} primes drawn uniformly from [1e5, 3e6] (numpy default_rng(4)), smallest "
                     f"7-smooth even N with p/N <= 19.5, {iters} iterations from S0=4",
@@ -466,6 +478,7 @@ def batched_leg(gl, dev: int, iters: int) -> dict:
         "speedup_vs_sequential_plain": seq_plain / t, "speedup_vs_sequential_fused": seq_fused / t,
         "sequential_note": "one test at a time: sum over tests of iterations x the form's ms/iteration at "
                            "that N, measured over 200 L2-warm iterations per distinct N (CUDA events)",
+        "sequential_check": check,
     }
 
 
@@ -500,10 +513,20 @@ def served_leg(gl, dev: int, window: int) -> dict:
         "steps": srv.stats["steps"], "batch_rebuilds": srv.stats["rebuilds"], "lanes": srv.stats["lanes"],
     }
     out.update({k: v for k, v in ours.items()})
+    checks = [r for r in reqs if not r.full][:12]
     for name, mode in (("plain", gl.MODE_PLAIN), ("fused", gl.MODE_FUSED)):
         ms = serve.measure_ms_per_iter(pairs, mode, device=dev, iters=200)
         seq = serve.latency_summary(serve.sequential_schedule(reqs, lambda r: ms[Nmap[r.rid]]))
         out[f"sequential_{name}"] = {k: seq[k] for k in ("tests_per_h", "p50_s", "p99_s", "makespan_s")}
+        # measured check of the model on the first 12 Res64 checks, run one at a time
+        meas = sum(serve.run_sequential([(r.p, Nmap[r.rid], r.iterations) for r in checks], mode, device=dev))
+        model = sum(r.iterations * ms[Nmap[r.rid]] for r in checks) * 1e-3
+        out[f"sequential_{name}"]["check"] = {"requests": len(checks), "model_s": model, "measured_s": meas,
+                                              "measured_over_model": meas / model}
+        if mode == gl.MODE_FUSED:
+            out["lead_lane_slowdown"] = serve.lane_slowdown(done, ms, "lead")
+            out["lead_lane_slowdown"]["note"] = ("in-mix time (admission to completion) over alone time "
+                                                 "(iterations x fused ms/iteration at that N)")
     out["speedup_tests_per_h_vs_sequential_plain"] = ours["tests_per_h"] / out["sequential_plain"]["tests_per_h"]
     out["sequential_note"] = ("one test at a time in arrival order: iterations x the form's ms/iteration at "
                               "that N, measured over 200 L2-warm iterations per distinct N (CUDA events)")

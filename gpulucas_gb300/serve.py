@@ -297,3 +297,27 @@ def measure_ms_per_iter(ps_Ns: Iterable[tuple[int, int]], mode: int, device: int
             rep = pl.iterate(iters, check=False)
             out[N] = rep.ms / iters
     return out
+
+
+def run_sequential(tests: Sequence[tuple[int, int, int]], mode: int, device: int = 0) -> list[float]:
+    """Run (p, N, iterations) tests one at a time, each from S0 = 4 in its own plan, and
+    return each one's device time in seconds (the library's CUDA-event timing of its
+    iterations).  The measured check of the one-test-at-a-time comparators."""
+    import gpulucas_gb300 as gl
+    out = []
+    for p, N, iters in tests:
+        with gl.Plan(p, N, mode=mode, device=device) as pl:
+            pl.reset()
+            rep = pl.iterate(iters, check=False)
+            out.append(rep.ms * 1e-3)
+    return out
+
+
+def lane_slowdown(done: Sequence[Completion], ms_per_iter: dict[int, float], lane: str = "lead") -> dict:
+    """In-mix time (admission to completion) over alone time (iterations x the fused
+    form's ms/iteration at that N) of the tests that ran in `lane`."""
+    r = [(c.done_s - c.admit_s) / (c.iterations * ms_per_iter[c.N] * 1e-3)
+         for c in done if c.lane == lane and c.status == GL_OK and c.N in ms_per_iter]
+    if not r:
+        return dict(tests=0)
+    return dict(tests=len(r), mean=statistics.fmean(r), max=max(r), min=min(r))

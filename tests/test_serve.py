@@ -238,3 +238,15 @@ def test_serve_lead_lane_holds_longest_chain():
     for c in done.values():
         assert c.status == serve.GL_OK and c.res64 == _exact(c.p, c.iterations)
     assert done[0].is_prime and done[1].is_prime and done[2].is_prime
+
+
+def test_lane_slowdown_from_completions():
+    """In-mix over alone time of the tests one lane ran (alone = iterations x ms/iteration)."""
+    from gpulucas_gb300 import serve
+    C = serve.Completion
+    done = [C(1, 101, 4096, 1000, True, 0.0, 1.0, 3.0, 0, False, False, 0.0, 0, lane="lead"),
+            C(2, 103, 8192, 2000, True, 0.0, 0.5, 4.5, 0, False, False, 0.0, 0, lane="lead"),
+            C(3, 107, 4096, 500, False, 0.0, 0.0, 9.0, 0, False, False, 0.0, 0, lane="bulk")]
+    r = serve.lane_slowdown(done, {4096: 1.0, 8192: 1.0}, "lead")
+    assert r["tests"] == 2 and abs(r["mean"] - 2.0) < 1e-12 and r["max"] == 2.0
+    assert serve.lane_slowdown(done, {4096: 1.0}, "chain") == {"tests": 0}
