@@ -1025,9 +1025,9 @@ int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, i
     pl->iters_done += iters;
     pl->carry_valid = pl->mode == GL_MODE_PLAIN;
   }
-  const int rc = ensure_carry(pl);
-  if (rc != GL_OK) return rc;
-  GL_CUDA(launch_add_carry(pl->args, pl->stream));
+  if (pl->carry_valid) GL_CUDA(launch_add_carry(pl->args, pl->stream));
+  else GL_CUDA(launch_dice_words(pl->args, pl->mode == GL_MODE_FUSED, pl->stream));
+  pl->carry_valid = true;  // (words, 0) is the carry-save state
   GL_CUDA(cudaMemcpyAsync(words_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));

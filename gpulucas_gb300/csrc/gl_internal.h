@@ -144,6 +144,8 @@ cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
 cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
 // (digit, hi) -> (digit + hi[j-1], 0): the carry-added words, the same state
 cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s);
+// products -> (carry-added words, 0) in one pass (colmajor_layout: the fused form's layout)
+cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s);
 // fused form: natural <-> column-major copies of an int64 word array
 cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
                                  cudaStream_t s);

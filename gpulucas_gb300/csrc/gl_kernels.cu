@@ -773,6 +773,35 @@ __global__ void k_add_carry(IterArgs a) {
   a.digit[j] += (int)a.hi[j == 0 ? a.N - 1 : j - 1];
 }
 
+// The carry-added words straight from the products: word j is the digit of j's digit sum
+// plus the carry of word j-1's (each thread dices both), and the carries are cleared.  One
+// pass instead of dicing, adding the carries and clearing them.  CM: the fused form's
+// column-major products and flags.
+template <bool CM>
+__global__ void k_dice_words(IterArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = a.N;
+  if (j >= N) return;
+  auto pos = [&](int k) {
+    if (k < 0) k += N;
+    return CM ? colmajor(a, k) : k;
+  };
+  const uint32_t fj = a.flags[pos(j)], fm = a.flags[pos(j - 1)];
+  const long long sj = dice_sum(a.LO, a.n, fj, [&](int i) { return a.ll[pos(j - i)]; });
+  const long long sm = dice_sum(a.LO, a.n, fm, [&](int i) { return a.ll[pos(j - 1 - i)]; });
+  int dj, hj, dm, hm;
+  balanced_split(sj, a.LO + (int)(fj & 1), &dj, &hj);
+  balanced_split(sm, a.LO + (int)(fm & 1), &dm, &hm);
+  a.digit[j] = dj + hm;
+  a.hi[j] = 0;
+}
+
+cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s) {
+  if (colmajor_layout) k_dice_words<true><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  else k_dice_words<false><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s) {
   k_add_carry<<<(a.N + 255) / 256, 256, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
