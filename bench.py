@@ -338,7 +338,8 @@ def run_ours(args, world: int, rank: int, local: int):
         "config": {"workload": WORKLOAD,
                    "p": P3, "N": N3, "fft": f"{info.fft_h} x {info.fft_w}", "parallelism": "replicas",
                    "layout": {"radix_h": [r for r in info.radix_h if r], "radix_w": [r for r in info.radix_w if r],
-                              "column_variant": info.col_variant, "threads_col": info.threads_col,
+                              "column_variant": info.col_variant, "row_variant": info.row_variant,
+                              "threads_col": info.threads_col,
                               "threads_row": info.threads_row},
                    "l2": "flushed before every timed step (512 MiB write); the test's ~170 MB of state and "
                          "tables exceed the 129 MB L2 anyway",

@@ -1,7 +1,7 @@
 """Command line with the reference's flags (gpuLucas.cu:374-454):
 
     python -m gpulucas_gb300 [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain]
-                             [-H h] [-I mode] [-R radix] [p]
+                             [-H h] [-I mode] [-R radix] [-P mode] [p]
 
 -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); without -f the length is chosen as
         findSignalSize does (gpuLucas.cu:1064-1187)
@@ -16,6 +16,8 @@
         3 two columns per CTA, 4 two columns per CTA forward + prefetched weights inverse,
         -1 two-buffer (the layout search picks among these otherwise)
 -R r    fused form, with -H: largest radix of the row DFTs (8, 4 or 2)
+-P mode fused form, with -H: row pass compiled for any radix (-1), or for radices 4, 3, 2
+        only with its stage values in shared memory (1) or read through L1 (2)
 SIGINT / SIGTERM write a checkpoint and exit (gpuLucas.cu:365-369, 1425-1429).
 A full test appends the reference's result line to results.txt (gpuLucas.cu:1514-1548)
 and removes its checkpoint files (gpuLucas.cu:628-632).
@@ -50,6 +52,7 @@ def main(argv=None) -> int:
     ap.add_argument("-H", type=int, default=0)
     ap.add_argument("-I", type=int, default=0, choices=[-1, 0, 1, 2, 3, 4])
     ap.add_argument("-R", type=int, default=0, choices=[0, 2, 4, 8])
+    ap.add_argument("-P", type=int, default=0, choices=[-1, 0, 1, 2])
     ap.add_argument("p", nargs="?", type=int, default=0)
     a = ap.parse_args(argv)
     if a.h:
@@ -83,7 +86,8 @@ def main(argv=None) -> int:
     signal.signal(signal.SIGINT, _on_signal)
     signal.signal(signal.SIGTERM, _on_signal)
     t0 = time.time()
-    with gl.Plan(p, N, mode=mode, device=a.d, fft_h=a.H, col_inplace=a.I, max_radix_row=a.R) as pl:
+    with gl.Plan(p, N, mode=mode, device=a.d, fft_h=a.H, col_inplace=a.I, max_radix_row=a.R,
+                 row_pass=a.P) as pl:
         i = pl.info
         if resume_k is not None:
             pl.resume(chk)
@@ -97,7 +101,8 @@ def main(argv=None) -> int:
             rw = "x".join(str(r) for r in i.radix_w if r)
             rh = "x".join(str(r) for r in i.radix_h if r)
             print(f"Testing M{p}, word sizes ({i.lo_bits}, {i.hi_bits}), FFT length {N} "
-                  f"({i.fft_h} x {i.fft_w} complex, columns {rh}, rows {rw}, column passes -I {i.col_variant}), "
+                  f"({i.fft_h} x {i.fft_w} complex, columns {rh}, rows {rw}, column passes -I {i.col_variant}, "
+                  f"row pass -P {i.row_variant}), "
                   f"carry depth {i.carry_depth}, form {a.m}")
         step = a.c if a.c > 0 else max(1, total - done)
         ms_total, maxerr = 0.0, 0.0

@@ -170,7 +170,7 @@ int row_threads(int W, const LinePlan& pw, int t0) {
 // largest radix is rc (columns) / rr (rows); each column gets one thread per butterfly
 // of its largest-radix stage, each row pair row_threads().
 int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRadix, int rr = kMaxRadix,
-                      bool ip = false, bool pf = false, bool ws = false) {
+                      bool ip = false, bool pf = false, bool ws = false, int row = 0) {
   if ((rc != 8 && rc != 4 && rc != 2) || (rr != 8 && rr != 4 && rr != 2)) return GL_ERR_ARG;
   int bestH = 0;
   for (const auto& c : ranked_layouts(M, sms))
@@ -196,6 +196,16 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   };
   g->t_col = threads(g->H, rc, kMaxThreads);
   g->t_row = row_threads(g->W, g->pw, threads(2 * g->W, rr, kRowThreads));
+  g->row_var = 0;
+  if (row < 0 || row > 2) return GL_ERR_ARG;
+  if (row > 0) {
+    for (int s = 0; s < g->pw.nst; ++s) {
+      const int R = g->pw.radix[s];
+      if (R != 2 && R != 3 && R != 4) return GL_ERR_SIZE;
+    }
+    g->row_var = row;
+    if (row == 2) g->sm_row = (size_t)4 * g->ls_row * 16;  // stage values read through L1
+  }
   g->col_ip = 0;
   g->col_pf = 0;
   g->col_ws = 0;
@@ -248,10 +258,10 @@ int stage_offsets(const LinePlan& lp, int* off) {
 
 // Device time of one fused iteration with column length H, measured on zero-filled
 // buffers (the kernels' time does not depend on the values).  Returns ms, or -1.
-double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, bool ws, int n, int sms, int iters,
+double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, bool ws, int row, int n, int sms, int iters,
                    cudaStream_t s) {
   FusedGeom g{};
-  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip, pf, ws) != GL_OK) return -1.0;
+  if (choose_fused_geom(M, H, sms, &g, rc, rr, ip, pf, ws, row) != GL_OK) return -1.0;
   const int N = 2 * M;
   const int szw = stage_offsets(g.pw, g.pw.off), szh = stage_offsets(g.ph, g.ph.off);
   const size_t bytes[] = {sizeof(long long) * N, (size_t)N, (size_t)N, sizeof(double) * N, sizeof(double) * N,
@@ -302,7 +312,7 @@ double time_layout(int M, int H, int rc, int rr, bool ip, bool pf, bool ws, int 
 // idle when 2W/8 is not a multiple of 32 (W = 576: 144 butterflies on 192 threads), while
 // radix-4 stages fill whole warps.
 struct TunedLayout {
-  int H = 0, rc = kMaxRadix, rr = kMaxRadix;
+  int H = 0, rc = kMaxRadix, rr = kMaxRadix, row = 0;
   bool ip = false, pf = false, ws = false;
   double ms = 0.0;
 };
@@ -322,8 +332,8 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
   TunedLayout best;
   double best_ms = 1e300;
   const int iters = M >= (1 << 18) ? 10 : 40;
-  auto consider = [&](int H, int rc, int rr, bool ip, bool pf = false, bool ws = false) {
-    const double ms = time_layout(M, H, rc, rr, ip, pf, ws, n, sms, iters, s);
+  auto consider = [&](int H, int rc, int rr, bool ip, bool pf = false, bool ws = false, int row = 0) {
+    const double ms = time_layout(M, H, rc, rr, ip, pf, ws, row, n, sms, iters, s);
     if (ms > 0.0 && ms < best_ms) {
       best_ms = ms;
       best.H = H;
@@ -332,6 +342,7 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
       best.ip = ip;
       best.pf = pf;
       best.ws = ws;
+      best.row = row;
     }
   };
   for (size_t i = 0; i < ranked.size() && i < 6; ++i) {
@@ -348,6 +359,13 @@ TunedLayout autotune_layout(int M, int n, int sms, cudaStream_t s, double* ms_ou
   if (M >= (1 << 17) && best.H) {
     const TunedLayout b = best;
     consider(b.H, b.rc, 4, b.ip, b.pf, b.ws);
+  }
+  if (best.H) {
+    // the row pass compiled for radices 4, 3, 2 only, with its stage values in shared
+    // memory or read through L1 (where the row plan allows it; otherwise not timed)
+    const TunedLayout b = best;
+    consider(b.H, b.rc, b.rr, b.ip, b.pf, b.ws, 1);
+    consider(b.H, b.rc, b.rr, b.ip, b.pf, b.ws, 2);
   }
   if (M < (1 << 17))
     for (size_t i = 0; i < ranked.size() && i < 3; ++i) {
@@ -584,6 +602,7 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
   }
   if (o.resident > 0 && !resident) return GL_ERR_SIZE;
   bool col_ip = false, col_pf = false, col_ws = false;
+  int row_var = 0;
   if (o.mode == GL_MODE_FUSED && !force_h && o.autotune && !sms_override) {
     const TunedLayout t = autotune_layout(M, n, sms, 0, nullptr);
     if (t.H) {
@@ -593,7 +612,12 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
       col_ip = t.ip && !resident;
       col_pf = col_ip && t.pf;
       col_ws = col_ip && t.ws;
+      row_var = resident ? 0 : t.row;
     }
+  }
+  if (o.row_pass) {
+    if (o.row_pass < -1 || o.row_pass > 2) return GL_ERR_ARG;
+    row_var = o.row_pass > 0 && !resident ? o.row_pass : 0;
   }
   if (o.col_inplace) {
     if (o.col_inplace > 4) return GL_ERR_ARG;
@@ -601,8 +625,9 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     col_pf = col_ip && (o.col_inplace == 2 || o.col_inplace == 4);
     col_ws = col_ip && (o.col_inplace == 3 || o.col_inplace == 4);
   }
-  int rc = o.mode == GL_MODE_FUSED ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf, col_ws)
-                                   : choose_plain_geom(M, &pg);
+  int rc = o.mode == GL_MODE_FUSED
+               ? choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, col_ip, col_pf, col_ws, row_var)
+               : choose_plain_geom(M, &pg);
   if (rc == GL_ERR_SIZE && col_ip && o.col_inplace <= 0)  // the searched layout cannot: two buffers
     rc = choose_fused_geom(M, force_h, sms, &fg, cap_c, cap_r, false);
   if (rc != GL_OK) return rc;
@@ -721,8 +746,10 @@ int gl_plan_create_ex(int p, int N, const gl_plan_opts* opts, int sms_override, 
     GL_TRYC(cudaStreamSynchronize(pl->stream));  // host tables go out of scope
     a.W = W; a.H = H; a.G = 1; a.pw = pl->fg.pw; a.ph = pl->fg.ph; a.ls_col = fg.ls_col; a.ls_row = fg.ls_row;
     a.twW_n = (int)twW.size();
-    // the row pass copies the whole table behind its four line buffers
-    if ((size_t)4 * fg.ls_row * 16 + twW.size() * sizeof(DevCplx) != fg.sm_row) GL_TRY(GL_ERR_SIZE);
+    // the row pass copies the whole table behind its four line buffers (unless it reads
+    // the table through L1)
+    if ((size_t)4 * fg.ls_row * 16 + (fg.row_var == 2 ? 0 : twW.size() * sizeof(DevCplx)) != fg.sm_row)
+      GL_TRY(GL_ERR_SIZE);
     GL_TRYC(set_fused_smem_limits(fg));
     if (resident) {
       if (rg.twH_n != (int)twH.size() || rg.twW_n != (int)twW.size()) GL_TRY(GL_ERR_SIZE);
@@ -796,6 +823,7 @@ int gl_plan_get_info(const gl_plan* pl, gl_plan_info* info) {
   if (pl->mode == GL_MODE_FUSED) {
     info->fft_w = pl->fg.W; info->fft_h = pl->fg.H; info->cols_per_cta = pl->fg.col_ws ? 2 : pl->fg.G;
     info->col_variant = !pl->fg.col_ip ? -1 : pl->fg.col_ws ? (pl->fg.col_pf ? 4 : 3) : (pl->fg.col_pf ? 2 : 1);
+    info->row_variant = pl->fg.row_var ? pl->fg.row_var : -1;
     for (int i = 0; i < pl->fg.pw.nst; ++i) info->radix_w[i] = pl->fg.pw.radix[i];
     for (int i = 0; i < pl->fg.ph.nst; ++i) info->radix_h[i] = pl->fg.ph.radix[i];
     info->threads_col = pl->fg.t_col; info->threads_row = pl->fg.t_row;

@@ -29,7 +29,7 @@ void on_signal(int) { g_stop = 1; }
 void usage() {
   std::fprintf(stderr,
                "usage: gpulucas [-h] [-v] [-q] [-f N] [-n p] [-d dev] [-c freq] [-k iters] [-m fused|plain] "
-               "[-H h] [-I mode] [-R radix] [p]\n"
+               "[-H h] [-I mode] [-R radix] [-P mode] [p]\n"
                "  -f N    FFT length (even, N/2 = 2^a 3^b 5^c 7^d); default: timed search\n"
                "  -n p    exponent of 2^p - 1 (or give it as the last argument)\n"
                "  -d dev  CUDA device\n"
@@ -40,6 +40,7 @@ void usage() {
                "  -I mode column passes: 1 in place, 2 in place + prefetch, 3 two columns per CTA,\n"
                "          4 two columns per CTA forward + prefetch inverse, -1 two buffers\n"
                "  -R r    largest radix of the row DFTs (8, 4 or 2)\n"
+               "  -P mode row pass: -1 any radix, 1 radices 4/3/2 only, 2 the same with L1 stage values\n"
                "  -v -q   verbose / quiet\n");
 }
 
@@ -58,7 +59,7 @@ int fail(const char* what, int st) {
 
 int main(int argc, char** argv) {
   bool verbose = false, quiet = false;
-  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED, inplace = 0, row_radix = 0;
+  int N = 0, p = 0, dev = 0, fft_h = 0, mode = GL_MODE_FUSED, inplace = 0, row_radix = 0, row_pass = 0;
   long long freq = 0, k = 0;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
@@ -82,6 +83,7 @@ int main(int argc, char** argv) {
     else if (a == "-H") fft_h = std::atoi(next("-H"));
     else if (a == "-I") inplace = std::atoi(next("-I"));
     else if (a == "-R") row_radix = std::atoi(next("-R"));
+    else if (a == "-P") row_pass = std::atoi(next("-P"));
     else if (a == "-m") {
       const std::string m = next("-m");
       if (m == "fused") mode = GL_MODE_FUSED;
@@ -124,6 +126,7 @@ int main(int argc, char** argv) {
   o.fft_h = fft_h;
   o.col_inplace = inplace;
   o.max_radix_row = row_radix;
+  o.row_pass = row_pass;
   if (!N) {
     double ms = 0.0, err = 0.0;
     const int st = gl_find_signal_size(p, &o, &N, &ms, &err);

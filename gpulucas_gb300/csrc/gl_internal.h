@@ -54,6 +54,9 @@ struct FusedGeom {
                              // (2 t_col threads, two in-place line buffers); while one half
                              // transforms its column the other dices or rounds its own (the
                              // inverse pass keeps one column per CTA when col_pf is set)
+  int row_var;               // row pass: 0 any radices; 1 radices 4, 3, 2 only (fewer
+                             // registers); 2 the same reading its stage values through L1
+                             // (no shared-memory copy)
   int rc, rr;                // largest radix of the column / row line plans (8, 4 or 2):
                              // a smaller cap means more, shorter butterflies per stage and
                              // so more threads per line, for lengths too short to fill the GPU

@@ -119,15 +119,22 @@ __device__ __forceinline__ void stockham_stage(const cplx* __restrict__ src, cpl
 }
 
 // Transforms nlines lines held in `a` (line stride ls) using `b` as the second buffer;
-// returns the buffer that holds the result.
-template <int S, typename TW>
+// returns the buffer that holds the result.  R43: the plan has only radices 4, 3 and 2, and
+// only those stages are compiled (a kernel's registers are set by its largest stage).
+template <int S, bool R43 = false, typename TW>
 __device__ __forceinline__ cplx* line_fft(cplx* a, cplx* b, int nlines, int ls, const LinePlan& lp,
                                           const TW* tw) {
   int Ns = 1;
   for (int s = 0; s < lp.nst; ++s) {
     const TW* st = tw + lp.off[s];
     static_assert(kMaxRadix == 8, "line plans use radices 2, 4, 8, 3, 5, 7");
-    switch (lp.radix[s]) {
+    if (R43) {
+      switch (lp.radix[s]) {
+        case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+        case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+        default: stockham_stage<3, S>(a, b, nlines, ls, lp.L, Ns, st); break;
+      }
+    } else switch (lp.radix[s]) {
       case 8: stockham_stage<8, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 4: stockham_stage<4, S>(a, b, nlines, ls, lp.L, Ns, st); break;
       case 2: stockham_stage<2, S>(a, b, nlines, ls, lp.L, Ns, st); break;
@@ -374,9 +381,11 @@ __global__ void __launch_bounds__(2 * kMaxThreads, 2) k_col_fwd_ws(IterArgs a) {
   col_fwd_store(a, second ? c1 : c0, buf, g.tid, half);
 }
 
-// The row pass's stage values (17.4 KB at W = 576) are copied into shared memory behind
+// The row pass's stage values (17.7 KB at W = 576) are copied into shared memory behind
 // the four line buffers by one bulk copy, issued before the rows are loaded so the two
 // overlap; both DFTs of the pair, forward and inverse, then read them from shared memory.
+// L1TW: they are read through L1 instead (no copy, that much less shared memory per CTA).
+template <bool R43 = false, bool L1TW = false>
 __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 .. H/2 */) {
   extern __shared__ cplx smem[];
   __shared__ alignas(8) uint64_t tw_bar;
@@ -387,24 +396,33 @@ __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 
   const int nl = self ? 1 : 2;
   cplx* buf1 = smem + 2 * ls;
   cplx* tws = smem + 4 * ls;
-  if (threadIdx.x == 0) mbar_init(&tw_bar);
-  __syncthreads();
-  if (threadIdx.x == 0) bulk_load(tws, a.twW, (uint32_t)a.twW_n * (uint32_t)sizeof(DevCplx), &tw_bar);
+  if (!L1TW) {
+    if (threadIdx.x == 0) mbar_init(&tw_bar);
+    __syncthreads();
+    if (threadIdx.x == 0) bulk_load(tws, a.twW, (uint32_t)a.twW_n * (uint32_t)sizeof(DevCplx), &tw_bar);
+  }
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
     const int l = idx >= W;
     const int k1 = idx - l * W;
     smem[l * ls + pad(k1)] = ldc(a.Z + (size_t)(l ? rb : ra) * W + k1);
   }
-  const bool ok = mbar_wait(&tw_bar, 0);
-  if (__syncthreads_or(!ok)) {
-    if (threadIdx.x == 0) {
-      atomicOr(&a.status->flags, kStatusTimeout);
-      mbar_wait(&tw_bar, 0);  // the copy may still land in this CTA's shared memory
+  if (L1TW) {
+    __syncthreads();
+  } else {
+    const bool ok = mbar_wait(&tw_bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&a.status->flags, kStatusTimeout);
+        mbar_wait(&tw_bar, 0);  // the copy may still land in this CTA's shared memory
+      }
+      return;
     }
-    return;
   }
-  const cplx* twc = tws;
-  cplx* sp = line_fft<-1>(smem, buf1, nl, ls, a.pw, twc);
+  const auto twc = [&] {
+    if constexpr (L1TW) return a.twW;
+    else return static_cast<const cplx*>(tws);
+  }();
+  cplx* sp = line_fft<-1, R43>(smem, buf1, nl, ls, a.pw, twc);
   cplx* other = sp == smem ? buf1 : smem;
   const DevCplx* twp = a.twPair + (size_t)ra * W;
   if (!self) {
@@ -435,7 +453,7 @@ __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 
     }
   }
   __syncthreads();
-  const cplx* res = line_fft<+1>(sp, other, nl, ls, a.pw, twc);
+  const cplx* res = line_fft<+1, R43>(sp, other, nl, ls, a.pw, twc);
   for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
     const int l = idx >= W;
     const int m1 = idx - l * W;
@@ -445,6 +463,12 @@ __device__ __forceinline__ void row_sq_body(const IterArgs& a, const int c /* 0 
 }
 
 __global__ void __launch_bounds__(kRowThreads, 3) k_row_sq(IterArgs a) { row_sq_body(a, blockIdx.x); }
+// Row plans of radices 4, 3 and 2 only: 64 registers or fewer, so four CTAs of 256 threads
+// fit an SM's registers, and with L1TW its shared memory too.
+template <bool L1TW>
+__global__ void __launch_bounds__(kRowThreads, 4) k_row_sq43(IterArgs a) {
+  row_sq_body<true, L1TW>(a, blockIdx.x);
+}
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll
@@ -678,6 +702,10 @@ cudaError_t set_fused_smem_limits(const FusedGeom& g) {
     return e;
   if ((e = cudaFuncSetAttribute(k_col_inv<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
     return e;
+  if ((e = cudaFuncSetAttribute(k_row_sq43<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_row_sq43<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem)))
+    return e;
   return cudaFuncSetAttribute(k_row_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
 }
 
@@ -718,17 +746,23 @@ static void launch_col_inv(const IterArgs& a, const FusedGeom& g, cudaStream_t s
   else k_col_inv<false, false><<<a.W, g.t_col, g.sm_cinv, s>>>(a);
 }
 
+static void launch_row(const IterArgs& a, const FusedGeom& g, cudaStream_t s) {
+  if (g.row_var == 2) k_row_sq43<true><<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+  else if (g.row_var == 1) k_row_sq43<false><<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+  else k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+}
+
 cudaError_t launch_fused_iteration(const IterArgs& a, const FusedGeom& g, cudaStream_t s, bool from_state) {
   if (from_state) launch_col_fwd<true>(a, g, s);
   else launch_col_fwd<false>(a, g, s);
-  k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+  launch_row(a, g, s);
   launch_col_inv(a, g, s);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fused_kernel(const IterArgs& a, const FusedGeom& g, cudaStream_t s, int which) {
   if (which == 0) launch_col_fwd<false>(a, g, s);
-  else if (which == 1) k_row_sq<<<a.H / 2 + 1, g.t_row, g.sm_row, s>>>(a);
+  else if (which == 1) launch_row(a, g, s);
   else launch_col_inv(a, g, s);
   return cudaGetLastError();
 }

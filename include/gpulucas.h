@@ -70,7 +70,10 @@ typedef struct {
                               block, so that one half's dicing or rounding overlaps the other
                               half's DFT; 4: 3 for the forward pass, 2 for the inverse pass;
                               0 = the autotuner decides, -1 = never */
-    int reserved[1];
+    int row_pass;          /* fused form: the row pass compiled for any radix (-1), or, for
+                              row plans of radices 4, 3 and 2 only, compiled for those (1:
+                              stage values in shared memory; 2: read through L1, so more
+                              CTAs fit an SM); 0 = the autotuner decides */
 } gl_plan_opts;
 
 typedef struct {
@@ -90,6 +93,7 @@ typedef struct {
     int col_variant;       /* fused form: the column passes as a col_inplace value (-1 two
                               buffers, 1 in place, 2 + prefetched weights, 3 two columns per
                               CTA, 4 two columns forward + prefetched weights inverse) */
+    int row_variant;       /* fused form: the row pass as a row_pass value (-1, 1, 2) */
 } gl_plan_info;
 
 typedef struct {

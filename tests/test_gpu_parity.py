@@ -167,6 +167,33 @@ def test_two_column_passes_match_oracle(gl, orc, p, N, variant):
         assert a.res64() == b.res64()
 
 
+@pytest.mark.parametrize("p,N", [(2000003, 131072), (645131, 36864), (43112609, 2359296)],
+                         ids=["W32", "W9", "C3"])
+@pytest.mark.parametrize("row_pass", [1, 2], ids=["r43-shared", "r43-l1"])
+def test_row_pass_variants_match_oracle(gl, orc, p, N, row_pass):
+    """The row pass compiled for radices 4, 3, 2 only (row plans 4·4·2, 3·3, 4·4·4·3·3), with
+    its stage values in shared memory or read through L1, gives the products of the generic
+    row pass and of the oracle."""
+    H = 2048
+    with gl.Plan(p, N, row_pass=row_pass, max_radix_row=4, fft_h=H, autotune=0) as a, \
+            gl.Plan(p, N, row_pass=-1, max_radix_row=4, fft_h=H, autotune=0) as b:
+        assert a.info.row_variant == row_pass and b.info.row_variant == -1
+        if row_pass == 2:
+            assert a.info.smem_row < b.info.smem_row
+        a.iterate(7)
+        b.iterate(7)
+        pa = a.products()
+        assert (pa == b.products()).all()
+        if N <= 163840:
+            assert (pa == orc.IBDWT(p, N).iterate(7).ll()).all()
+
+
+def test_row_pass_variant_refused_for_other_radices(gl):
+    """A row plan with a radix-8 stage cannot take the radix-4/3/2 row pass."""
+    with pytest.raises(gl.GLError):
+        gl.Plan(43112609, 2359296, row_pass=1, max_radix_row=8, fft_h=2048, autotune=0)
+
+
 @pytest.mark.parametrize("p,N", [(44497, 2048), (1000003, 54432), (2976221, 163840)])
 @pytest.mark.parametrize("caps", [(4, 4), (2, 2), (4, 8), (8, 2)])
 def test_radix_capped_layouts_match_oracle(gl, orc, p, N, caps):
