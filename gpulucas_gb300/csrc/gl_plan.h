@@ -29,6 +29,11 @@ struct gl_plan {
   bool carry_valid = true;     // device (digit, hi) matches the current products
   cudaGraphExec_t gexec = nullptr;
   int gexec_iters = 0;
+  // gl_iterate_host_words, one iteration between pinned host buffers: the whole step
+  // (copy in, from-state iteration, dicing into words, copy out) as one graph
+  cudaGraphExec_t hw_exec = nullptr;
+  const void* hw_in = nullptr;
+  void* hw_out = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t device_bytes = 0;
   bool resident = false;        // short length: whole check intervals in one cluster

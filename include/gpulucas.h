@@ -174,7 +174,9 @@ int gl_iterate_host(gl_plan* plan, const int32_t* digit_in, const int8_t* hi_in,
  * (IrrBaseBalanced.cu:117-125).  Loading words w continues exactly as the carry-save
  * state it came from (the next FFT input is the same), and the words returned are the
  * carry-save state after the iterations with its carries added.  words_in may alias
- * words_out. */
+ * words_out.  With pinned buffers and iters == 1 (a caller stepping one iteration at a
+ * time) the whole step runs as one CUDA graph, built on the first call for these buffers
+ * and kept by the plan. */
 int gl_iterate_host_words(gl_plan* plan, const int32_t* words_in, int64_t iters, int32_t* words_out,
                           gl_iter_report* report);
 /* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */

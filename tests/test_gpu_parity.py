@@ -340,6 +340,38 @@ def test_iterate_host_pinned_buffers(gl, orc, p, N, mode):
             assert (d.numpy() == d2).all() and (h.numpy() == h2).all()
 
 
+@pytest.mark.parametrize("p,N", [(1000003, 54432), (43112609, 2359296)])
+def test_iterate_host_words_pinned_graph(gl, orc, p, N):
+    """Pinned buffers and one iteration per call take the captured-step path (one graph per
+    plan and buffer pair): in place step after step, then into a second buffer (the graph
+    is rebuilt), the words equal those of the same steps through pageable buffers, and
+    the iteration count and products follow."""
+    import ctypes
+
+    import torch
+    w0 = np.zeros(N, np.int32)
+    w0[0] = 4
+    a = torch.from_numpy(w0.copy()).pin_memory()
+    b = torch.empty(N, dtype=torch.int32).pin_memory()
+    ap, bp = ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr())
+    rep = gl.IterReport()
+    with gl.Plan(p, N) as pl, gl.Plan(p, N) as ref:
+        w = w0.copy()
+        for step in range(3):
+            assert gl.lib.gl_iterate_host_words(pl._h, ap, 1, ap, ctypes.byref(rep)) == 0
+            assert rep.iterations == 1 and rep.total_iterations == step + 1
+            w, _ = ref.iterate_host_words(w, 1)
+            assert (a.numpy() == w).all(), step
+        assert gl.lib.gl_iterate_host_words(pl._h, ap, 1, bp, ctypes.byref(rep)) == 0
+        w, _ = ref.iterate_host_words(w, 1)
+        assert (b.numpy() == w).all()
+        assert (pl.products() == ref.products()).all()
+        if N <= 163840:
+            o = orc.IBDWT(p, N).iterate(4)
+            d, h = o.state()
+            assert (b.numpy() == d + np.roll(h.astype(np.int32), 1)).all()
+
+
 def test_bounded_wait_times_out_and_device_stays_usable(gl, orc):
     """A kernel waiting on a barrier that nothing completes gives up after its bound,
     the host reads GL_ERR_TIMEOUT, and the context keeps working (no trap, no hang)."""
