@@ -1037,17 +1037,20 @@ int gl_iterate_host(gl_plan* pl, const int32_t* digit_in, const int8_t* hi_in, i
   return st;
 }
 
-static bool pinned_host(const void* p) {
+// The device address of pinned (page-locked, mapped) host memory, or null for any other
+// pointer.
+static void* mapped_host(const void* p) {
   cudaPointerAttributes at{};
   const bool ok = cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost;
   cudaGetLastError();  // a failed query leaves no error behind
-  return ok;
+  return ok ? at.devicePointer : nullptr;
 }
 
-// One host-state step of one fused iteration: words in, the state-loading iteration,
-// words out, the status out.  Enqueued on the plan's stream (captured into a graph by the
-// caller).
-static cudaError_t enqueue_words_step(gl_plan* pl, const int32_t* words_in, int32_t* words_out) {
+// One host-state step of one fused iteration: words in, the state-loading iteration, the
+// dicing into words, which also stores the words and the status into the mapped host
+// buffers (out_dev, status_dev: their device addresses).  Enqueued on the plan's stream
+// (captured into a graph by the caller).
+static cudaError_t enqueue_words_step(gl_plan* pl, const int32_t* words_in, int32_t* out_dev, Status* status_dev) {
   const size_t N = (size_t)pl->N;
   cudaError_t e;
   if ((e = cudaMemcpyAsync(pl->args.digit, words_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream)))
@@ -1055,10 +1058,7 @@ static cudaError_t enqueue_words_step(gl_plan* pl, const int32_t* words_in, int3
   if ((e = cudaMemsetAsync(pl->args.hi, 0, N, pl->stream))) return e;
   if ((e = cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream))) return e;
   if ((e = launch_fused_iteration(pl->args, pl->fg, pl->stream, true))) return e;
-  if ((e = launch_dice_words(pl->args, true, pl->stream))) return e;
-  if ((e = cudaMemcpyAsync(words_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream)))
-    return e;
-  return cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream);
+  return launch_dice_words(pl->args, true, pl->stream, out_dev, status_dev);
 }
 
 int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, int32_t* words_out,
@@ -1066,15 +1066,17 @@ int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, i
   if (!pl || !words_in || !words_out || iters < 0) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));
   const size_t N = (size_t)pl->N;
-  if (iters == 1 && pl->mode == GL_MODE_FUSED && !pl->resident && pl->use_graphs && pinned_host(words_in) &&
-      pinned_host(words_out)) {
+  void* out_dev = nullptr;
+  Status* status_dev = nullptr;
+  if (iters == 1 && pl->mode == GL_MODE_FUSED && !pl->resident && pl->use_graphs && mapped_host(words_in) &&
+      (out_dev = mapped_host(words_out)) && (status_dev = (Status*)mapped_host(pl->h_status))) {
     // the step as one graph launch (about ten calls fewer per step), kept for these buffers
-    if (!pl->hw_exec || pl->hw_in != words_in || pl->hw_out != words_out) {
+    if (!pl->hw_exec || pl->hw_in != words_in || pl->hw_out != words_out || pl->hw_out_dev != out_dev) {
       if (pl->hw_exec) cudaGraphExecDestroy(pl->hw_exec);
       pl->hw_exec = nullptr;
       cudaGraph_t graph = nullptr;
       GL_CUDA(cudaStreamBeginCapture(pl->stream, cudaStreamCaptureModeThreadLocal));
-      const cudaError_t es = enqueue_words_step(pl, words_in, words_out);
+      const cudaError_t es = enqueue_words_step(pl, words_in, (int32_t*)out_dev, status_dev);
       const cudaError_t ec = cudaStreamEndCapture(pl->stream, &graph);
       if (es != cudaSuccess || ec != cudaSuccess || !graph) {
         if (graph) cudaGraphDestroy(graph);
@@ -1088,6 +1090,7 @@ int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, i
       }
       pl->hw_in = words_in;
       pl->hw_out = words_out;
+      pl->hw_out_dev = out_dev;
     }
     GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
     GL_CUDA(cudaGraphLaunch(pl->hw_exec, pl->stream));

@@ -147,8 +147,11 @@ cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
 cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
 // (digit, hi) -> (digit + hi[j-1], 0): the carry-added words, the same state
 cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s);
-// products -> (carry-added words, 0) in one pass (colmajor_layout: the fused form's layout)
-cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s);
+// products -> (carry-added words, 0) in one pass (colmajor_layout: the fused form's layout);
+// host_words / host_status, when not null, are device addresses of mapped pinned host
+// memory that receive the words and the status as well
+cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s,
+                              int32_t* host_words = nullptr, Status* host_status = nullptr);
 // fused form: natural <-> column-major copies of an int64 word array
 cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long long* dst, bool to_colmajor,
                                  cudaStream_t s);

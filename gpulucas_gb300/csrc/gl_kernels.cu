@@ -810,11 +810,14 @@ __global__ void k_add_carry(IterArgs a) {
 // The carry-added words straight from the products: word j is the digit of j's digit sum
 // plus the carry of word j-1's (each thread dices both), and the carries are cleared.  One
 // pass instead of dicing, adding the carries and clearing them.  CM: the fused form's
-// column-major products and flags.
+// column-major products and flags.  host_words / host_status (device addresses of mapped
+// pinned host memory, or null): the words and the status are also stored there, so the
+// transfer to the host runs under the dicing instead of as copies after it.
 template <bool CM>
-__global__ void k_dice_words(IterArgs a) {
+__global__ void k_dice_words(IterArgs a, int32_t* host_words, Status* host_status) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int N = a.N;
+  if (host_status && j == 0) *host_status = *a.status;  // final: the passes before have ended
   if (j >= N) return;
   auto pos = [&](int k) {
     if (k < 0) k += N;
@@ -828,11 +831,13 @@ __global__ void k_dice_words(IterArgs a) {
   balanced_split(sm, a.LO + (int)(fm & 1), &dm, &hm);
   a.digit[j] = dj + hm;
   a.hi[j] = 0;
+  if (host_words) host_words[j] = dj + hm;
 }
 
-cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s) {
-  if (colmajor_layout) k_dice_words<true><<<(a.N + 255) / 256, 256, 0, s>>>(a);
-  else k_dice_words<false><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+cudaError_t launch_dice_words(const IterArgs& a, bool colmajor_layout, cudaStream_t s, int32_t* host_words,
+                              Status* host_status) {
+  if (colmajor_layout) k_dice_words<true><<<(a.N + 255) / 256, 256, 0, s>>>(a, host_words, host_status);
+  else k_dice_words<false><<<(a.N + 255) / 256, 256, 0, s>>>(a, host_words, host_status);
   return cudaGetLastError();
 }
 

@@ -30,10 +30,12 @@ struct gl_plan {
   cudaGraphExec_t gexec = nullptr;
   int gexec_iters = 0;
   // gl_iterate_host_words, one iteration between pinned host buffers: the whole step
-  // (copy in, from-state iteration, dicing into words, copy out) as one graph
+  // (copy in, from-state iteration, dicing into words stored straight into the mapped
+  // output buffer and status) as one graph, kept for one pair of buffers
   cudaGraphExec_t hw_exec = nullptr;
   const void* hw_in = nullptr;
   void* hw_out = nullptr;
+  void* hw_out_dev = nullptr;  // device address of hw_out's mapping
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t device_bytes = 0;
   bool resident = false;        // short length: whole check intervals in one cluster

@@ -176,7 +176,10 @@ int gl_iterate_host(gl_plan* plan, const int32_t* digit_in, const int8_t* hi_in,
  * carry-save state after the iterations with its carries added.  words_in may alias
  * words_out.  With pinned buffers and iters == 1 (a caller stepping one iteration at a
  * time) the whole step runs as one CUDA graph, built on the first call for these buffers
- * and kept by the plan. */
+ * and kept by the plan; in it the kernel that forms the words stores them (and the
+ * round-off status) straight into the mapped output buffer, so that transfer runs under
+ * the kernel instead of as a copy after it.  Both buffers must hold N words until the
+ * call returns. */
 int gl_iterate_host_words(gl_plan* plan, const int32_t* words_in, int64_t iters, int32_t* words_out,
                           gl_iter_report* report);
 /* Set a carry-save state (balanced digits + int8 carries) and its iteration count. */
