@@ -995,11 +995,126 @@ static int ensure_carry(gl_plan* pl) {
   return GL_OK;
 }
 
+// The device address of pinned (page-locked, mapped) host memory, or null for any other
+// pointer.
+static void* mapped_host(const void* p) {
+  cudaPointerAttributes at{};
+  const bool ok = cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // a failed query leaves no error behind
+  return ok ? at.devicePointer : nullptr;
+}
+
+// One host-state step of one fused iteration between pinned host buffers.  kind 1: the
+// state as carry-added words (in[0] -> out[0]); kind 2: as the carry-save pair (digit
+// in[0], carry in[1] -> out[0], out[1]).  out_dev: device addresses of the outputs'
+// mappings.
+struct HostStep {
+  int kind;
+  const void* in[2];
+  void* out[2];
+  void* out_dev[2];
+};
+
+// Copies in, the state-loading iteration, and the dicing, which also stores the state and
+// the status into the mapped host buffers, so that transfer runs under the kernel instead
+// of as copies after it.  Enqueued on the plan's stream (captured into a graph by the
+// caller).
+static cudaError_t enqueue_host_step(gl_plan* pl, const HostStep& hs, Status* status_dev) {
+  const size_t N = (size_t)pl->N;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(pl->args.digit, hs.in[0], sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream)))
+    return e;
+  if (hs.kind == 1) e = cudaMemsetAsync(pl->args.hi, 0, N, pl->stream);
+  else e = cudaMemcpyAsync(pl->args.hi, hs.in[1], N, cudaMemcpyHostToDevice, pl->stream);
+  if (e) return e;
+  if ((e = cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream))) return e;
+  if ((e = launch_fused_iteration(pl->args, pl->fg, pl->stream, true))) return e;
+  if (hs.kind == 1) return launch_dice_words(pl->args, true, pl->stream, (int32_t*)hs.out_dev[0], status_dev);
+  return launch_dice_perm(pl->args, pl->stream, (int*)hs.out_dev[0], (signed char*)hs.out_dev[1], status_dev);
+}
+
+// Whether this call runs as the captured step: one iteration of a fused (not resident)
+// plan with graphs, every buffer pinned and mapped.  Fills hs->out_dev and *status_dev.
+static bool host_step_mapped(gl_plan* pl, int64_t iters, HostStep* hs, Status** status_dev) {
+  if (iters != 1 || pl->mode != GL_MODE_FUSED || pl->resident || !pl->use_graphs) return false;
+  for (int i = 0; i < (hs->kind == 1 ? 1 : 2); ++i)
+    if (!mapped_host(hs->in[i]) || !(hs->out_dev[i] = mapped_host(hs->out[i]))) return false;
+  return (*status_dev = (Status*)mapped_host(pl->h_status)) != nullptr;
+}
+
+// Records the start event and launches the step as one graph (about ten calls fewer per
+// step), built on the first call for these buffers and kept by the plan.
+static int launch_host_step(gl_plan* pl, const HostStep& hs, Status* status_dev) {
+  bool same = pl->hw_exec && pl->hw_kind == hs.kind;
+  for (int i = 0; i < 2; ++i)
+    same = same && pl->hw_in[i] == hs.in[i] && pl->hw_out[i] == hs.out[i] && pl->hw_out_dev[i] == hs.out_dev[i];
+  if (!same) {
+    if (pl->hw_exec) cudaGraphExecDestroy(pl->hw_exec);
+    pl->hw_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    GL_CUDA(cudaStreamBeginCapture(pl->stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t es = enqueue_host_step(pl, hs, status_dev);
+    const cudaError_t ec = cudaStreamEndCapture(pl->stream, &graph);
+    if (es != cudaSuccess || ec != cudaSuccess || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      return GL_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&pl->hw_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      pl->hw_exec = nullptr;
+      return GL_ERR_CUDA;
+    }
+    pl->hw_kind = hs.kind;
+    for (int i = 0; i < 2; ++i) {
+      pl->hw_in[i] = hs.in[i];
+      pl->hw_out[i] = hs.out[i];
+      pl->hw_out_dev[i] = hs.out_dev[i];
+    }
+  }
+  GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
+  GL_CUDA(cudaGraphLaunch(pl->hw_exec, pl->stream));
+  pl->from_state = false;
+  pl->iters_done += 1;
+  pl->carry_valid = true;  // the device (digit, hi) is the state the host received
+  return GL_OK;
+}
+
+// The end of a host-state call whose work is enqueued after ev0: wait for it, read the
+// status it left in pl->h_status, report.
+static int finish_host_step(gl_plan* pl, int64_t iters, gl_iter_report* rep) {
+  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
+  GL_CUDA(cudaEventSynchronize(pl->ev1));
+  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
+  if (e > pl->run_maxerr) pl->run_maxerr = e;
+  int st = GL_OK;
+  if (pl->h_status->flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
+  else if (pl->h_status->flags) st = GL_ERR_OVERFLOW;
+  else if (e >= pl->error_limit) st = GL_ERR_ROUNDOFF;
+  float ms = 0.f;
+  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
+  if (rep) {
+    rep->iterations = iters;
+    rep->total_iterations = pl->iters_done;
+    rep->max_roundoff = e;
+    rep->ms = ms;
+    rep->status = st;
+  }
+  return st;
+}
+
 int gl_iterate_host(gl_plan* pl, const int32_t* digit_in, const int8_t* hi_in, int64_t iters, int32_t* digit_out,
                     int8_t* hi_out, gl_iter_report* rep) {
   if (!pl || !digit_in || !hi_in || !digit_out || !hi_out || iters < 0) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));
   const size_t N = (size_t)pl->N;
+  HostStep hs{2, {digit_in, hi_in}, {digit_out, hi_out}, {nullptr, nullptr}};
+  Status* status_dev = nullptr;
+  if (host_step_mapped(pl, iters, &hs, &status_dev)) {
+    const int rc = launch_host_step(pl, hs, status_dev);
+    if (rc != GL_OK) return rc;
+    return finish_host_step(pl, iters, rep);
+  }
   GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
   GL_CUDA(cudaMemcpyAsync(pl->args.digit, digit_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream));
   GL_CUDA(cudaMemcpyAsync(pl->args.hi, hi_in, N, cudaMemcpyHostToDevice, pl->stream));
@@ -1017,48 +1132,7 @@ int gl_iterate_host(gl_plan* pl, const int32_t* digit_in, const int8_t* hi_in, i
   GL_CUDA(cudaMemcpyAsync(digit_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaMemcpyAsync(hi_out, pl->args.hi, N, cudaMemcpyDeviceToHost, pl->stream));
   GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
-  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
-  GL_CUDA(cudaEventSynchronize(pl->ev1));
-  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
-  if (e > pl->run_maxerr) pl->run_maxerr = e;
-  int st = GL_OK;
-  if (pl->h_status->flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
-  else if (pl->h_status->flags) st = GL_ERR_OVERFLOW;
-  else if (e >= pl->error_limit) st = GL_ERR_ROUNDOFF;
-  float ms = 0.f;
-  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
-  if (rep) {
-    rep->iterations = iters;
-    rep->total_iterations = pl->iters_done;
-    rep->max_roundoff = e;
-    rep->ms = ms;
-    rep->status = st;
-  }
-  return st;
-}
-
-// The device address of pinned (page-locked, mapped) host memory, or null for any other
-// pointer.
-static void* mapped_host(const void* p) {
-  cudaPointerAttributes at{};
-  const bool ok = cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost;
-  cudaGetLastError();  // a failed query leaves no error behind
-  return ok ? at.devicePointer : nullptr;
-}
-
-// One host-state step of one fused iteration: words in, the state-loading iteration, the
-// dicing into words, which also stores the words and the status into the mapped host
-// buffers (out_dev, status_dev: their device addresses).  Enqueued on the plan's stream
-// (captured into a graph by the caller).
-static cudaError_t enqueue_words_step(gl_plan* pl, const int32_t* words_in, int32_t* out_dev, Status* status_dev) {
-  const size_t N = (size_t)pl->N;
-  cudaError_t e;
-  if ((e = cudaMemcpyAsync(pl->args.digit, words_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream)))
-    return e;
-  if ((e = cudaMemsetAsync(pl->args.hi, 0, N, pl->stream))) return e;
-  if ((e = cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream))) return e;
-  if ((e = launch_fused_iteration(pl->args, pl->fg, pl->stream, true))) return e;
-  return launch_dice_words(pl->args, true, pl->stream, out_dev, status_dev);
+  return finish_host_step(pl, iters, rep);
 }
 
 int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, int32_t* words_out,
@@ -1066,74 +1140,31 @@ int gl_iterate_host_words(gl_plan* pl, const int32_t* words_in, int64_t iters, i
   if (!pl || !words_in || !words_out || iters < 0) return GL_ERR_ARG;
   GL_CUDA(cudaSetDevice(pl->device));
   const size_t N = (size_t)pl->N;
-  void* out_dev = nullptr;
+  HostStep hs{1, {words_in, nullptr}, {words_out, nullptr}, {nullptr, nullptr}};
   Status* status_dev = nullptr;
-  if (iters == 1 && pl->mode == GL_MODE_FUSED && !pl->resident && pl->use_graphs && mapped_host(words_in) &&
-      (out_dev = mapped_host(words_out)) && (status_dev = (Status*)mapped_host(pl->h_status))) {
-    // the step as one graph launch (about ten calls fewer per step), kept for these buffers
-    if (!pl->hw_exec || pl->hw_in != words_in || pl->hw_out != words_out || pl->hw_out_dev != out_dev) {
-      if (pl->hw_exec) cudaGraphExecDestroy(pl->hw_exec);
-      pl->hw_exec = nullptr;
-      cudaGraph_t graph = nullptr;
-      GL_CUDA(cudaStreamBeginCapture(pl->stream, cudaStreamCaptureModeThreadLocal));
-      const cudaError_t es = enqueue_words_step(pl, words_in, (int32_t*)out_dev, status_dev);
-      const cudaError_t ec = cudaStreamEndCapture(pl->stream, &graph);
-      if (es != cudaSuccess || ec != cudaSuccess || !graph) {
-        if (graph) cudaGraphDestroy(graph);
-        return GL_ERR_CUDA;
-      }
-      const cudaError_t ei = cudaGraphInstantiate(&pl->hw_exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (ei != cudaSuccess) {
-        pl->hw_exec = nullptr;
-        return GL_ERR_CUDA;
-      }
-      pl->hw_in = words_in;
-      pl->hw_out = words_out;
-      pl->hw_out_dev = out_dev;
-    }
-    GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
-    GL_CUDA(cudaGraphLaunch(pl->hw_exec, pl->stream));
-    pl->from_state = false;
-    pl->iters_done += 1;
-    pl->carry_valid = true;  // (words, 0) is the carry-save state
-  } else {
-    GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
-    GL_CUDA(cudaMemcpyAsync(pl->args.digit, words_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream));
-    GL_CUDA(cudaMemsetAsync(pl->args.hi, 0, N, pl->stream));
-    GL_CUDA(cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream));
-    pl->from_state = pl->mode == GL_MODE_FUSED;
-    pl->carry_valid = true;
-    if (iters > 0) {
-      const int rc = enqueue(pl, iters);
-      if (rc != GL_OK) return rc;
-      pl->iters_done += iters;
-      pl->carry_valid = pl->mode == GL_MODE_PLAIN;
-    }
-    if (pl->carry_valid) GL_CUDA(launch_add_carry(pl->args, pl->stream));
-    else GL_CUDA(launch_dice_words(pl->args, pl->mode == GL_MODE_FUSED, pl->stream));
-    pl->carry_valid = true;  // (words, 0) is the carry-save state
-    GL_CUDA(cudaMemcpyAsync(words_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
-    GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
+  if (host_step_mapped(pl, iters, &hs, &status_dev)) {
+    const int rc = launch_host_step(pl, hs, status_dev);
+    if (rc != GL_OK) return rc;
+    return finish_host_step(pl, iters, rep);
   }
-  GL_CUDA(cudaEventRecord(pl->ev1, pl->stream));
-  GL_CUDA(cudaEventSynchronize(pl->ev1));
-  const double e = std::ldexp((double)pl->h_status->maxerr64, -64);
-  if (e > pl->run_maxerr) pl->run_maxerr = e;
-  int st = GL_OK;
-  if (pl->h_status->flags & kStatusTimeout) st = GL_ERR_TIMEOUT;
-  else if (pl->h_status->flags) st = GL_ERR_OVERFLOW;
-  else if (e >= pl->error_limit) st = GL_ERR_ROUNDOFF;
-  float ms = 0.f;
-  GL_CUDA(cudaEventElapsedTime(&ms, pl->ev0, pl->ev1));
-  if (rep) {
-    rep->iterations = iters;
-    rep->total_iterations = pl->iters_done;
-    rep->max_roundoff = e;
-    rep->ms = ms;
-    rep->status = st;
+  GL_CUDA(cudaEventRecord(pl->ev0, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->args.digit, words_in, sizeof(int32_t) * N, cudaMemcpyHostToDevice, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.hi, 0, N, pl->stream));
+  GL_CUDA(cudaMemsetAsync(pl->args.status, 0, sizeof(Status), pl->stream));
+  pl->from_state = pl->mode == GL_MODE_FUSED;
+  pl->carry_valid = true;
+  if (iters > 0) {
+    const int rc = enqueue(pl, iters);
+    if (rc != GL_OK) return rc;
+    pl->iters_done += iters;
+    pl->carry_valid = pl->mode == GL_MODE_PLAIN;
   }
-  return st;
+  if (pl->carry_valid) GL_CUDA(launch_add_carry(pl->args, pl->stream));
+  else GL_CUDA(launch_dice_words(pl->args, pl->mode == GL_MODE_FUSED, pl->stream));
+  pl->carry_valid = true;  // (words, 0) is the carry-save state
+  GL_CUDA(cudaMemcpyAsync(words_out, pl->args.digit, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, pl->stream));
+  GL_CUDA(cudaMemcpyAsync(pl->h_status, pl->args.status, sizeof(Status), cudaMemcpyDeviceToHost, pl->stream));
+  return finish_host_step(pl, iters, rep);
 }
 
 int gl_get_carry_state(gl_plan* pl, int32_t* digit_out, int8_t* hi_out) {

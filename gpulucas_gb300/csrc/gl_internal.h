@@ -143,8 +143,11 @@ cudaError_t launch_plain_iteration(const IterArgs& a, const PlainGeom& g, cudaSt
 cudaError_t launch_set_initial(const IterArgs& a, int mode, cudaStream_t s);
 // carry-save state (digit, hi) = dice(ll) for the fused form; plain keeps it already
 cudaError_t launch_dice(const IterArgs& a, cudaStream_t s);
-// fused form: dice the column-major products into natural-order (digit, hi)
-cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s);
+// fused form: dice the column-major products into natural-order (digit, hi); host_digit,
+// host_hi and host_status, when not null, are device addresses of mapped pinned host
+// memory that receive the state and the status as well
+cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s, int* host_digit = nullptr,
+                             signed char* host_hi = nullptr, Status* host_status = nullptr);
 // (digit, hi) -> (digit + hi[j-1], 0): the carry-added words, the same state
 cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s);
 // products -> (carry-added words, 0) in one pass (colmajor_layout: the fused form's layout);

@@ -783,9 +783,12 @@ cudaError_t launch_permute_words(const IterArgs& a, const long long* src, long l
   return cudaGetLastError();
 }
 
-// llintToIrrBal<n> over column-major products (fused form), natural-order output
-__global__ void k_dice_perm(IterArgs a) {
+// llintToIrrBal<n> over column-major products (fused form), natural-order output.
+// host_digit / host_hi / host_status (device addresses of mapped pinned host memory, or
+// null): the carry-save state and the status are also stored there.
+__global__ void k_dice_perm(IterArgs a, int* host_digit, signed char* host_hi, Status* host_status) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (host_status && j == 0) *host_status = *a.status;  // final: the passes before have ended
   if (j >= a.N) return;
   const int N = a.N;
   const uint32_t f = a.flags[colmajor(a, j)];
@@ -797,6 +800,10 @@ __global__ void k_dice_perm(IterArgs a) {
   balanced_split(s, a.LO + (int)(f & 1), &d, &h);
   a.digit[j] = d;
   a.hi[j] = (signed char)h;
+  if (host_digit) {
+    host_digit[j] = d;
+    host_hi[j] = (signed char)h;
+  }
 }
 
 // digit[j] += hi[j-1 mod N] (addPseudoBalanced, IrrBaseBalanced.cu:117-125); the caller
@@ -848,8 +855,9 @@ cudaError_t launch_add_carry(const IterArgs& a, cudaStream_t s) {
   return cudaMemsetAsync(a.hi, 0, (size_t)a.N, s);
 }
 
-cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s) {
-  k_dice_perm<<<(a.N + 255) / 256, 256, 0, s>>>(a);
+cudaError_t launch_dice_perm(const IterArgs& a, cudaStream_t s, int* host_digit, signed char* host_hi,
+                             Status* host_status) {
+  k_dice_perm<<<(a.N + 255) / 256, 256, 0, s>>>(a, host_digit, host_hi, host_status);
   return cudaGetLastError();
 }
 

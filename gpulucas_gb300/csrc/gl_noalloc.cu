@@ -99,6 +99,15 @@ extern "C" int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* l
   if (pg.nst <= 0) return GL_ERR_SIZE;
   pg.threads = 256;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    // the call waits for its stream, which a stream being captured into a graph cannot do
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      return GL_ERR_CUDA;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return GL_ERR_ARG;
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GL_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return GL_ERR_ARG;

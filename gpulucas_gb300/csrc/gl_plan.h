@@ -29,13 +29,14 @@ struct gl_plan {
   bool carry_valid = true;     // device (digit, hi) matches the current products
   cudaGraphExec_t gexec = nullptr;
   int gexec_iters = 0;
-  // gl_iterate_host_words, one iteration between pinned host buffers: the whole step
-  // (copy in, from-state iteration, dicing into words stored straight into the mapped
-  // output buffer and status) as one graph, kept for one pair of buffers
+  // gl_iterate_host_words / gl_iterate_host, one iteration between pinned host buffers:
+  // the whole step (copies in, from-state iteration, dicing stored straight into the
+  // mapped output buffers and status) as one graph, kept for one set of buffers
   cudaGraphExec_t hw_exec = nullptr;
-  const void* hw_in = nullptr;
-  void* hw_out = nullptr;
-  void* hw_out_dev = nullptr;  // device address of hw_out's mapping
+  int hw_kind = 0;                  // 1: words step, 2: carry-save pair step
+  const void* hw_in[2] = {nullptr, nullptr};
+  void* hw_out[2] = {nullptr, nullptr};
+  void* hw_out_dev[2] = {nullptr, nullptr};  // device addresses of hw_out's mappings
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t device_bytes = 0;
   bool resident = false;        // short length: whole check intervals in one cluster

@@ -165,7 +165,9 @@ int gl_set_products(gl_plan* plan, const int64_t* ll, int64_t iterations);
  * hi; N each, host buffers), runs `iters` iterations, and writes the resulting state
  * back, with one synchronisation for the whole call (the round-off of these iterations
  * is checked once, at the end).  digit_in/hi_in may alias digit_out/hi_out; pinned
- * buffers copy at the CPU link's full rate. */
+ * buffers copy at the CPU link's full rate.  With pinned buffers and iters == 1 the step
+ * runs as one CUDA graph kept by the plan, whose last kernel stores the state and the
+ * status straight into the mapped output buffers (as gl_iterate_host_words below). */
 int gl_iterate_host(gl_plan* plan, const int32_t* digit_in, const int8_t* hi_in, int64_t iters,
                     int32_t* digit_out, int8_t* hi_out, gl_iter_report* report);
 /* The same with the state as carry-added words, 4 bytes per word instead of 5: word j is
@@ -385,12 +387,12 @@ int gl_server_destroy(gl_server* server);
  * overlap only in part return GL_ERR_ARG), and stores the maximum round-off in
  * *max_roundoff.  It allocates nothing: its work arrays, tables and status word live in
  * a static device array sized for N <= 65536 (about 3.3 MiB, held on every GPU that
- * loads the library until exit); larger N returns GL_ERR_TOO_LARGE.  The first call on
- * a device sets up that device (looks up the array's address and uploads the test's
- * tables); make it before any stream capture on that device.  The call is synchronous:
- * it returns after `stream` has finished the iterations.  All calls share the array and
- * would race if they overlapped on the GPU; a lock held until the stream has finished
- * keeps the calls of one process from overlapping.
+ * loads the library until exit); larger N returns GL_ERR_TOO_LARGE.  A call with new
+ * (p, N) uploads that test's tables into the array first.  The call is synchronous: it
+ * returns after `stream` has finished the iterations, so it cannot be captured into a
+ * CUDA graph (on a stream that is capturing it returns GL_ERR_ARG and enqueues
+ * nothing).  All calls share the array; a lock held until the stream has finished keeps
+ * the calls of one process from overlapping on the GPU.
  * Returns GL_ERR_ROUNDOFF at round-off >= 0.4 and GL_ERR_OVERFLOW as gl_iterate. */
 int gl_iterate_noalloc(int p, int N, const int64_t* ll_in, int64_t* ll_out, int64_t iters,
                        double* max_roundoff, void* stream);

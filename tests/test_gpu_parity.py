@@ -372,6 +372,40 @@ def test_iterate_host_words_pinned_graph(gl, orc, p, N):
             assert (b.numpy() == d + np.roll(h.astype(np.int32), 1)).all()
 
 
+def test_host_steps_switch_between_words_and_pair(gl, orc):
+    """One plan alternating the two pinned host-state steps (carry-save pair, words, pair,
+    words): each call rebuilds the plan's captured step for its kind and buffers, and
+    every state equals the oracle's."""
+    import ctypes
+
+    import torch
+    p, N = 1000003, 54432
+    o = orc.IBDWT(p, N)
+    d0, h0 = o.state()
+    d = torch.from_numpy(np.ascontiguousarray(d0, np.int32)).pin_memory()
+    h = torch.from_numpy(np.ascontiguousarray(h0, np.int8)).pin_memory()
+    w = torch.empty(N, dtype=torch.int32).pin_memory()
+    dp, hp, wp = (ctypes.c_void_p(t.data_ptr()) for t in (d, h, w))
+    rep = gl.IterReport()
+    with gl.Plan(p, N) as pl:
+        for step in range(4):
+            if step % 2 == 0:
+                assert gl.lib.gl_iterate_host(pl._h, dp, hp, 1, dp, hp, ctypes.byref(rep)) == 0
+                o.iterate(1)
+                d2, h2 = o.state()
+                assert (d.numpy() == d2).all() and (h.numpy() == h2).all(), step
+                w.copy_(torch.from_numpy(d2 + np.roll(h2.astype(np.int32), 1)))
+            else:
+                assert gl.lib.gl_iterate_host_words(pl._h, wp, 1, wp, ctypes.byref(rep)) == 0
+                o.iterate(1)
+                d2, h2 = o.state()
+                assert (w.numpy() == d2 + np.roll(h2.astype(np.int32), 1)).all(), step
+                d.copy_(torch.from_numpy(d2))
+                h.copy_(torch.from_numpy(h2))
+            assert rep.status == 0 and rep.total_iterations == step + 1
+        assert (pl.products() == o.ll()).all()
+
+
 def test_bounded_wait_times_out_and_device_stays_usable(gl, orc):
     """A kernel waiting on a barrier that nothing completes gives up after its bound,
     the host reads GL_ERR_TIMEOUT, and the context keeps working (no trap, no hang)."""

@@ -81,3 +81,30 @@ def test_noalloc_rejects_partly_overlapping_buffers(gl):
         rc = gl.lib.gl_iterate_noalloc(44497, N, ctypes.c_void_p(base), ctypes.c_void_p(base + 8 * shift), 1,
                                        ctypes.byref(err), None)
         assert rc == gl.GL_ERR_ARG, shift
+
+
+def test_noalloc_refuses_a_capturing_stream(gl):
+    """The call waits for its stream, so on a stream that is being captured into a CUDA
+    graph it returns GL_ERR_ARG and enqueues nothing; the next call on a plain stream
+    works as before."""
+    import torch
+    p, N = 44497, 2048
+    ll0 = np.zeros(N, np.int64)
+    ll0[0] = 4
+    d = torch.from_numpy(ll0).cuda()
+    err = ctypes.c_double()
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    rcs = []
+    with torch.cuda.graph(graph, stream=side):
+        rcs.append(gl.lib.gl_iterate_noalloc(p, N, ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(d.data_ptr()), 3,
+                                             ctypes.byref(err), ctypes.c_void_p(side.cuda_stream)))
+        d.add_(0)
+    assert rcs == [gl.GL_ERR_ARG]
+    del graph
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy(), ll0)
+    gl.iterate_noalloc(p, N, d.data_ptr(), d.data_ptr(), 3, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy(), _plan_products(gl, p, N, ll0, 3, gl.MODE_PLAIN))
