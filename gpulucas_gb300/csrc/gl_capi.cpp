@@ -50,37 +50,89 @@ bool fill_line_plan(int L, LinePlan* lp, int max_radix = kMaxRadix) {
 
 int round_up32(int x) { return (x + 31) / 32 * 32; }
 
-// FP64 instructions per point of one line DFT with the given radices.  First stage:
+// FP64 instructions per point of one stage of radix r of a line DFT.  First stage:
 // constant twiddles only (layered DIT, DFT_R).  Later stages: radices 8, 4, 3 in ratio
 // form (66, 22, 16 instructions per butterfly), 2 and 16 the layered DIT (3 per point and
 // bit), 5 and 7 DFT_R plus one complex product per input.
+double stage_ops(int r, bool first) {
+  const bool pow2 = (r & (r - 1)) == 0;
+  int lg = 0;
+  while ((1 << lg) < r) ++lg;
+  if (!first && (r == 8 || r == 4 || r == 3)) return (r == 8 ? 66.0 : r == 4 ? 22.0 : 16.0) / r;
+  if (pow2) {
+    if (!first) return 3.0 * lg;
+    return r == 2 ? 2.0 : r == 4 ? 4.0 : r == 8 ? 6.5 : 9.25;  // 16
+  }
+  const double odd = r == 3 ? 14.0 : r == 5 ? 36.0 : 72.0;  // 7
+  return odd / r + (first ? 0.0 : 4.0 * (r - 1) / r);
+}
+
+// FP64 instructions per point of one line DFT with the given radices.
 double line_ops(const LinePlan& lp) {
-  auto first_pow2 = [](int r) {
-    switch (r) {
-      case 2: return 2.0;
-      case 4: return 4.0;
-      case 8: return 6.5;
-      default: return 9.25;  // 16
-    }
-  };
-  auto odd_ops = [](int r) {
-    switch (r) {
-      case 3: return 14.0;
-      case 5: return 36.0;
-      default: return 72.0;  // 7
-    }
-  };
+  double ops = 0.0;
+  for (int s = 0; s < lp.nst; ++s) ops += stage_ops(lp.radix[s], s == 0);
+  return ops;
+}
+
+// FP64 instructions issued per point of one line DFT when a CTA transforms `nlines` lines
+// of the plan together: a stage of radix r has nlines L / r butterflies, one per lane, and
+// a warp issues each instruction for all 32 lanes, so the stage costs round_up32(its
+// butterflies) / its butterflies times its work.
+double line_issue_ops(const LinePlan& lp, int nlines) {
   double ops = 0.0;
   for (int s = 0; s < lp.nst; ++s) {
-    const int r = lp.radix[s];
-    const bool pow2 = (r & (r - 1)) == 0;
-    int lg = 0;
-    while ((1 << lg) < r) ++lg;
-    if (s && (r == 8 || r == 4 || r == 3)) ops += (r == 8 ? 66.0 : r == 4 ? 22.0 : 16.0) / r;
-    else if (pow2) ops += s ? 3.0 * lg : first_pow2(r);
-    else ops += odd_ops(r) / r + (s ? 4.0 * (r - 1) / r : 0.0);
+    const int nb = nlines * lp.L / lp.radix[s];
+    ops += stage_ops(lp.radix[s], s == 0) * (double)((nb + 31) / 32 * 32) / nb;
   }
   return ops;
+}
+
+// Line plan that issues the fewest FP64 instructions with `nlines` lines per CTA, for
+// a batch member (lines short enough that partly filled warps matter): L = 2^a 3^b 5^c 7^d
+// with the power of two split into radices 8, 4 and 2 (8 and 4 up to max_radix) in every
+// way, and each distinct radix tried as the first stage (the one with constant twiddles);
+// the other stages keep the order 8, 4, 2, 3, 5, 7.  At most 8 stages.
+bool fill_line_plan_issue(int L, int nlines, int max_radix, LinePlan* lp) {
+  if (L < 2) return false;
+  int m = L, e[4] = {0, 0, 0, 0};
+  const int primes[4] = {2, 3, 5, 7};
+  for (int i = 0; i < 4; ++i)
+    while (m % primes[i] == 0) {
+      m /= primes[i];
+      ++e[i];
+    }
+  if (m != 1) return false;
+  double best = 1e300;
+  LinePlan out{};
+  for (int n8 = 0; 3 * n8 <= e[0]; ++n8) {
+    if (n8 && max_radix < 8) break;
+    for (int n4 = 0; 3 * n8 + 2 * n4 <= e[0]; ++n4) {
+      if (n4 && max_radix < 4) break;
+      const int n2 = e[0] - 3 * n8 - 2 * n4;
+      const int counts[6] = {n8, n4, n2, e[1], e[2], e[3]};
+      const int radices[6] = {8, 4, 2, 3, 5, 7};
+      const int nst = n8 + n4 + n2 + e[1] + e[2] + e[3];
+      if (nst < 1 || nst > 8) continue;
+      for (int f = 0; f < 6; ++f) {
+        if (!counts[f]) continue;
+        LinePlan c{};
+        c.L = L;
+        c.nst = nst;
+        int k = 0;
+        c.radix[k++] = radices[f];
+        for (int i = 0; i < 6; ++i)
+          for (int j = 0; j < counts[i] - (i == f ? 1 : 0); ++j) c.radix[k++] = radices[i];
+        const double cost = line_issue_ops(c, nlines);
+        if (cost < best - 1e-9) {
+          best = cost;
+          out = c;
+        }
+      }
+    }
+  }
+  if (best >= 1e300) return false;
+  *lp = out;
+  return true;
 }
 
 int padded_stride(int L) { return L + (L >> 4) + 1; }
@@ -121,16 +173,23 @@ std::vector<std::pair<double, int>> ranked_layouts(int M, int sms) {
     const int W = M / H;
     if (W < 4) continue;  // the forward column pass finds the words below a column with one wrap
     LinePlan a, b;
-    if (!fill_line_plan(W, &a) || !fill_line_plan(H, &b)) continue;
+    // a batch member: line plans and costs by the FP64 instructions issued (a CTA takes
+    // one column or one row pair), since its short lines leave warps partly filled
+    const bool member = sms == 1;
+    if (member ? !fill_line_plan_issue(W, 2, kMaxRadix, &a) || !fill_line_plan_issue(H, 1, kMaxRadix, &b)
+               : !fill_line_plan(W, &a) || !fill_line_plan(H, &b))
+      continue;
     const size_t smc = (size_t)2 * padded_stride(H) * 16, smr = row_smem(W, a);
     if (smc > (size_t)kMaxDynSmem || smr > (size_t)kMaxDynSmem) continue;
     if ((H + kElemsPerThread - 1) / kElemsPerThread > 4 * kMaxThreads) continue;
-    double col = std::ceil((double)W / sms) * H * (line_ops(b) + 6.0);
-    double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * line_ops(a) + 16.0);
-    if (sms == 1) {
-      // a batch member: its units share the device with the batch's other units, so the
-      // fixed cost of a CTA (launch, descriptor copy, barriers, global round trips) is
-      // charged per unit, which keeps the lines long enough to amortise it
+    const double col_ops = member ? line_issue_ops(b, 1) : line_ops(b);
+    const double row_ops = member ? line_issue_ops(a, 2) : line_ops(a);
+    double col = std::ceil((double)W / sms) * H * (col_ops + 6.0);
+    double row = std::ceil((double)(H / 2 + 1) / sms) * 2.0 * W * (2.0 * row_ops + 16.0);
+    if (member) {
+      // its units share the device with the batch's other units, so the fixed cost of a
+      // CTA (launch, descriptor copy, barriers, global round trips) is charged per unit,
+      // which keeps the lines long enough to amortise it
       col += (double)W * kBatchUnitOverhead;
       row += (double)(H / 2 + 1) * kBatchUnitOverhead;
     }
@@ -184,7 +243,11 @@ int choose_fused_geom(int M, int force_h, int sms, FusedGeom* g, int rc = kMaxRa
   g->G = 1;
   g->rc = rc;
   g->rr = rr;
-  if (!fill_line_plan(g->W, &g->pw, rr) || !fill_line_plan(g->H, &g->ph, rc)) return GL_ERR_SIZE;
+  if (sms == 1) {  // a batch member: the plans that issue the fewest FP64 instructions
+    if (!fill_line_plan_issue(g->W, 2, rr, &g->pw) || !fill_line_plan_issue(g->H, 1, rc, &g->ph)) return GL_ERR_SIZE;
+  } else if (!fill_line_plan(g->W, &g->pw, rr) || !fill_line_plan(g->H, &g->ph, rc)) {
+    return GL_ERR_SIZE;
+  }
   g->ls_col = padded_stride(g->H);
   g->ls_row = padded_stride(g->W);
   g->sm_col = (size_t)2 * g->ls_col * 16;
