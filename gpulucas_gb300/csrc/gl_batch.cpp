@@ -117,6 +117,12 @@ int read_status(gl_batch* b, double* worst_err) {
   return st;
 }
 
+// Row pairs per row-pass unit of a batch member: at most this many, within this much
+// shared memory per CTA (the unit's line buffers and stage values)
+constexpr int kMaxRowPairsPerUnit = 8;
+constexpr size_t kRowUnitSmem = 48 * 1024;
+constexpr int kRowUnitsPerSM = 16;
+
 // descriptor table, status array and unit maps of the batch's plans
 int assemble(gl_batch* b) {
   const int ntests = (int)b->plans.size();
@@ -156,11 +162,38 @@ int assemble(gl_batch* b) {
   });
   for (int t : order)
     for (int u = 0; u < b->plans[t]->fg.W; ++u) cols.push_back(make_int2(t, u));
+  // row units of k row pairs: as many pairs as the block takes in one round of the widest
+  // stage (the most butterflies), at most 8 and within kRowUnitSmem of shared memory, and
+  // only while the batch keeps kRowUnitsPerSM units per SM (a batch of a few tests needs
+  // one pair per CTA to spread its rows over the device)
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms < 1) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  long total_pairs = 0;
+  for (int i = 0; i < ntests; ++i) total_pairs += b->plans[i]->fg.H / 2 + 1;
+  const int kcap = (int)std::max(1L, std::min((long)kMaxRowPairsPerUnit, total_pairs / ((long)kRowUnitsPerSM * sms)));
+  std::vector<int> pairs((size_t)ntests, 1);
+  sm_row = 0;
+  for (int i = 0; i < ntests; ++i) {
+    const FusedGeom& g = b->plans[i]->fg;
+    int widest = 1;
+    for (int s = 0; s < g.pw.nst; ++s) widest = std::max(widest, 2 * g.W / g.pw.radix[s]);
+    const size_t lines = (size_t)4 * g.ls_row * 16, stage = g.sm_row - lines;
+    int k = std::max(1, std::min(kcap, t_row / widest));
+    while (k > 1 && (size_t)k * lines + stage > kRowUnitSmem) --k;
+    pairs[(size_t)i] = k;
+    sm_row = std::max(sm_row, (size_t)k * lines + stage);
+  }
   std::sort(order.begin(), order.end(), [&](int a, int c) {
-    return gl_plan_unit_cost(b->plans[a], true) > gl_plan_unit_cost(b->plans[c], true);
+    return gl_plan_unit_cost(b->plans[a], true) * pairs[(size_t)a] >
+           gl_plan_unit_cost(b->plans[c], true) * pairs[(size_t)c];
   });
-  for (int t : order)
-    for (int u = 0; u <= b->plans[t]->fg.H / 2; ++u) rows.push_back(make_int2(t, u));
+  for (int t : order) {
+    const int last = b->plans[t]->fg.H / 2, k = pairs[(size_t)t];
+    for (int c = 0; c <= last; c += k) rows.push_back(make_int2(t, c | (std::min(k, last + 1 - c) << 20)));
+  }
   int2 *d_cols = nullptr, *d_rows = nullptr;
   GB_TRY(upload(b, &d_cols, cols));
   GB_TRY(upload(b, &d_rows, rows));

@@ -633,12 +633,92 @@ __global__ void __launch_bounds__(kMaxThreads, 2) kb_col_fwd(const IterArgs* __r
   }
 }
 
+// Row pairs c0 .. c0 + k - 1 of one test in one CTA (a batch unit): pair i's rows c and
+// H - c are line slots 2i and 2i + 1, and all 2k lines go through each stage together, so
+// a short row's stages fill more of the block and the unit's fixed costs (descriptor,
+// stage values, barriers) are shared.  A self-paired row (c = 0 or H/2) has slot 2i only;
+// its slot 2i + 1 is zero-filled, transformed for nothing and not stored.  Every line's
+// arithmetic is row_sq_body's, so the products are the same bit for bit.
+__device__ __forceinline__ void row_sq_pairs(const IterArgs& a, const int c0, const int k) {
+  extern __shared__ cplx smem[];
+  __shared__ alignas(8) uint64_t tw_bar;
+  const int W = a.W, H = a.H;
+  const int ls = a.ls_row;
+  const int nl = 2 * k;
+  cplx* buf1 = smem + nl * ls;
+  cplx* tws = smem + 2 * nl * ls;
+  if (threadIdx.x == 0) mbar_init(&tw_bar);
+  __syncthreads();
+  if (threadIdx.x == 0) bulk_load(tws, a.twW, (uint32_t)a.twW_n * (uint32_t)sizeof(DevCplx), &tw_bar);
+  for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
+    const int l = idx / W;
+    const int k1 = idx - l * W;
+    const int c = c0 + (l >> 1);
+    const bool mirror = l & 1;
+    const bool self = c == 0 || 2 * c == H;
+    smem[l * ls + pad(k1)] = mirror && self ? mk(0.0, 0.0) : ldc(a.Z + (size_t)(mirror ? H - c : c) * W + k1);
+  }
+  {
+    const bool ok = mbar_wait(&tw_bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&a.status->flags, kStatusTimeout);
+        mbar_wait(&tw_bar, 0);  // the copy may still land in this CTA's shared memory
+      }
+      return;
+    }
+  }
+  const cplx* twc = tws;
+  cplx* sp = line_fft<-1>(smem, buf1, nl, ls, a.pw, twc);
+  cplx* other = sp == smem ? buf1 : smem;
+  for (int t = threadIdx.x; t < k * W; t += blockDim.x) {
+    const int i = t / W;
+    const int tt = t - i * W;
+    const int c = c0 + i;
+    cplx* la = sp + 2 * i * ls;
+    const DevCplx* twp = a.twPair + (size_t)c * W;
+    cplx vk, vkp;
+    if (c != 0 && 2 * c != H) {
+      const int tp = W - 1 - tt;
+      pair_square(la[pad(tt)], la[ls + pad(tp)], ld(twp + tt), &vk, &vkp);
+      la[pad(tt)] = vk;
+      la[ls + pad(tp)] = vkp;
+    } else if (c == 0) {
+      // row 0: frequency H*t pairs with H*((W - t) mod W)
+      if (tt > W / 2) continue;
+      const int tp = (W - tt) % W;
+      pair_square(la[pad(tt)], la[pad(tp)], ld(twp + tt), &vk, &vkp);
+      la[pad(tt)] = vk;
+      if (tp != tt) la[pad(tp)] = vkp;
+    } else {
+      // row H/2: frequency H/2 + H*t pairs with H/2 + H*(W-1-t)
+      if (tt >= (W + 1) / 2) continue;
+      const int tp = W - 1 - tt;
+      pair_square(la[pad(tt)], la[pad(tp)], ld(twp + tt), &vk, &vkp);
+      la[pad(tt)] = vk;
+      if (tp != tt) la[pad(tp)] = vkp;
+    }
+  }
+  __syncthreads();
+  const cplx* res = line_fft<+1>(sp, other, nl, ls, a.pw, twc);
+  for (int idx = threadIdx.x; idx < nl * W; idx += blockDim.x) {
+    const int l = idx / W;
+    const int m1 = idx - l * W;
+    const int c = c0 + (l >> 1);
+    const bool mirror = l & 1;
+    if (mirror && (c == 0 || 2 * c == H)) continue;
+    const int row = mirror ? H - c : c;
+    st(a.Z2 + (size_t)m1 * H + row, cmulc(res[l * ls + pad(m1)], ld(a.twK2 + (size_t)row * W + m1)));
+  }
+}
+
+// units[b] = (test, c0 | k << 20): the row pairs c0 .. c0 + k - 1 of that test
 __global__ void __launch_bounds__(kRowThreads, 3) kb_row_sq(const IterArgs* __restrict__ tests,
                                                             const int2* __restrict__ units) {
   __shared__ IterArgs sa;
   const int2 u = units[blockIdx.x];
   load_desc(tests, u.x, sa);
-  row_sq_body(sa, u.y);
+  row_sq_pairs(sa, u.y & ((1 << 20) - 1), u.y >> 20);
 }
 
 __global__ void __launch_bounds__(kMaxThreads, 3) kb_col_inv(const IterArgs* __restrict__ tests,
