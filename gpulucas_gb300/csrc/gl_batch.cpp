@@ -23,6 +23,11 @@ struct gl_batch {
   cudaStream_t stream = nullptr;
   std::vector<gl_plan*> plans;
   bool owns_plans = true;
+  // row-pass units of several row pairs for short-row members (gl_batch_create).  Off for
+  // batches over existing plans (the server's lanes): they share the device with
+  // higher-priority lanes, and longer-running CTAs there hold SMs the lead lane waits for
+  // (served p99 85.6 -> 91.7 s measured with them on)
+  bool merge_row_pairs = true;
   std::vector<void*> allocs;
   BatchLaunch launch{};
   Status* d_status = nullptr;
@@ -173,7 +178,9 @@ int assemble(gl_batch* b) {
   }
   long total_pairs = 0;
   for (int i = 0; i < ntests; ++i) total_pairs += b->plans[i]->fg.H / 2 + 1;
-  const int kcap = (int)std::max(1L, std::min((long)kMaxRowPairsPerUnit, total_pairs / ((long)kRowUnitsPerSM * sms)));
+  const int kcap = b->merge_row_pairs ? (int)std::max(1L, std::min((long)kMaxRowPairsPerUnit,
+                                                                 total_pairs / ((long)kRowUnitsPerSM * sms)))
+                                     : 1;
   std::vector<int> pairs((size_t)ntests, 1);
   sm_row = 0;
   for (int i = 0; i < ntests; ++i) {
@@ -338,6 +345,7 @@ int gl_batch_create_from_plans(gl_plan* const* plans, int nplans, const gl_plan_
     if (plans[i]->from_state) return GL_ERR_STATE;
   gl_batch* b = new gl_batch();
   b->owns_plans = false;
+  b->merge_row_pairs = false;
   b->device = plans[0]->device;
   b->check_every = o.check_every;
   b->error_limit = o.error_limit;

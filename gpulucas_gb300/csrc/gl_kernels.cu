@@ -712,13 +712,16 @@ __device__ __forceinline__ void row_sq_pairs(const IterArgs& a, const int c0, co
   }
 }
 
-// units[b] = (test, c0 | k << 20): the row pairs c0 .. c0 + k - 1 of that test
+// units[b] = (test, c0 | k << 20): the row pairs c0 .. c0 + k - 1 of that test (one pair:
+// the single-test row body)
 __global__ void __launch_bounds__(kRowThreads, 3) kb_row_sq(const IterArgs* __restrict__ tests,
                                                             const int2* __restrict__ units) {
   __shared__ IterArgs sa;
   const int2 u = units[blockIdx.x];
   load_desc(tests, u.x, sa);
-  row_sq_pairs(sa, u.y & ((1 << 20) - 1), u.y >> 20);
+  const int c0 = u.y & ((1 << 20) - 1), k = u.y >> 20;
+  if (k == 1) row_sq_body(sa, c0);
+  else row_sq_pairs(sa, c0, k);
 }
 
 __global__ void __launch_bounds__(kMaxThreads, 3) kb_col_inv(const IterArgs* __restrict__ tests,
