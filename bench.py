@@ -325,11 +325,12 @@ def run_ours(args, world: int, rank: int, local: int):
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": N3 * 4,
            "d2h_bytes_per_step": N3 * 4 + 16, "steps": e2e_steps,
            "path": "gl_iterate_host_words(plan, words, 1): H2D of the state as carry-added words "
-                   "(digit[j] + hi[j-1], int32), one iteration, D2H of the words and the round-off status, "
-                   "one synchronisation; pinned buffers",
+                   "(digit[j] + hi[j-1], int32), one iteration, D2H of the words and the round-off status "
+                   "(stored by the dicing kernel into the mapped pinned buffer), one synchronisation",
            "carry_save_pair": {"value": world * e2e_steps / cs_s, "unit": "iter/s",
                                "h2d_bytes_per_step": N3 * 5, "d2h_bytes_per_step": N3 * 5 + 16,
-                               "path": "gl_iterate_host(plan, digit, hi, 1): int32 digit + int8 carry"}}
+                               "path": "gl_iterate_host(plan, digit, hi, 1): int32 digit + int8 carry, "
+                                       "stored by the dicing kernel into the mapped pinned buffers"}}
     plan.close()
 
     line = {
